@@ -1,0 +1,744 @@
+// gemm_tc.cu -- the tensor-core GEMM for sm_103a.
+//
+// D(m,n) = alpha * sum_k op(A)(m,k) op(B)(k,n) + beta * C(m,n), column-major, fp32 accumulation in
+// TMEM.  This is the GB300 counterpart of TensileLite's generated MFMA kernel
+// (src/gemmMfmaKernelWriter.h:24-2073): the reference's fetch waves (global -> LDS ring,
+// :408-432/:1226-1400) become one TMA producer warp feeding a shared-memory ring guarded by
+// full/empty mbarriers; its math waves (LDS -> VGPR -> MFMA into AccVGPRs, :433-466/:1403-1547)
+// become one thread issuing tcgen05.mma from shared-memory descriptors into a TMEM accumulator;
+// its fused epilogue (beta*C pre-scaled, fma(alpha, acc, beta*C), convert, store; :1572-1768,
+// :1822-1906) becomes four warps draining TMEM with tcgen05.ld while the next tile accumulates into
+// the second TMEM buffer.
+//
+// Roles (192 threads, one CTA per SM, persistent over work units):
+//   warp 0     TMA producer: per k-block one box of B (128 n-rows) and one of A (bm m-rows)
+//   warp 1     TMEM allocator + MMA issuer (lane 0): 4 tcgen05.mma per k-block, commit -> empty
+//   warps 2-5  epilogue: TMEM lane = problem n, TMEM column = problem m, so each thread owns a
+//              contiguous run of m for one n -- column-major D rows are written as 16-byte vectors.
+// The problem's B^T is the MMA "A" operand (M = 128 along n) and A is the MMA "B" operand
+// (N = bm along m).  K-major operands (TN, the reference's layout) and MN-major operands (NN/NT)
+// are both read straight from global memory by TMA with 128-byte swizzling; no transpose pass.
+//
+// Work unit = (tile, k-split).  Split-k partials go to a workspace; the last CTA to finish a tile
+// (arrival counter) sums the partials in split order and runs the epilogue, so results do not
+// depend on scheduling.  The grouped variant walks a problem table with per-problem TMA maps.
+//
+// Every mbarrier wait is bounded (globaltimer); on expiry the kernel sets *err and returns.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <cstdio>
+#include <cstring>
+#include <type_traits>
+
+#include "ptx.cuh"
+#include "tl_internal.h"
+
+namespace tl {
+
+namespace {
+
+struct TcKernelParams {
+    CUtensorMap tmN, tmM, tmN_lo, tmM_lo;
+    const TcGroupEntry* group;
+    const int64_t* group_prefix;
+    int group_count;
+    void* D;
+    const void* C;
+    int64_t ldd, ldc, stride_d, stride_c;
+    int M, N, K, batch;
+    float alpha, beta;
+    int bm, stages, split_k, raster, x3;
+    int tiles_m, tiles_n;
+    int64_t total_work;
+    int num_kb;
+    int kb_elems;          // k elements per k-block (one 128-byte row)
+    uint32_t idesc;
+    uint32_t n_lbo, m_lbo, n_kstep, m_kstep;
+    int n_mn_major, m_mn_major;
+    int out_trunc;
+    float* ws;
+    int* counters;
+    int* err;
+    unsigned long long timeout_ns;
+};
+
+struct TileJob {
+    const void* tmN;
+    const void* tmM;
+    const void* tmN_lo;
+    const void* tmM_lo;
+    void* D;
+    const void* C;
+    int64_t ldd, ldc;
+    int M, N;
+    float alpha, beta;
+    int b, n0, m0;
+    int kb0, kb1;
+    int split;
+    int64_t tile;
+};
+
+__device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, TileJob& j)
+{
+    if (p.group == nullptr) {
+        const int64_t tile = w / p.split_k;
+        const int split = static_cast<int>(w % p.split_k);
+        const int64_t tpb = static_cast<int64_t>(p.tiles_m) * p.tiles_n;
+        const int b = static_cast<int>(tile / tpb);
+        const int64_t t = tile % tpb;
+        int in, jm;
+        if (p.raster > 0) {
+            const int64_t group_tiles = static_cast<int64_t>(p.raster) * p.tiles_m;
+            const int64_t g = t / group_tiles;
+            const int first_n = static_cast<int>(g * p.raster);
+            const int gsize = min(p.raster, p.tiles_n - first_n);
+            const int64_t r = t % group_tiles;
+            in = first_n + static_cast<int>(r % gsize);
+            jm = static_cast<int>(r / gsize);
+        } else {
+            in = static_cast<int>(t / p.tiles_m);
+            jm = static_cast<int>(t % p.tiles_m);
+        }
+        j.tmN = &p.tmN;
+        j.tmM = &p.tmM;
+        j.tmN_lo = &p.tmN_lo;
+        j.tmM_lo = &p.tmM_lo;
+        j.D = static_cast<char*>(p.D);
+        j.C = p.C;
+        j.ldd = p.ldd;
+        j.ldc = p.ldc;
+        j.M = p.M;
+        j.N = p.N;
+        j.alpha = p.alpha;
+        j.beta = p.beta;
+        j.b = b;
+        j.n0 = in * kTcTileN;
+        j.m0 = jm * p.bm;
+        j.kb0 = static_cast<int>((static_cast<int64_t>(split) * p.num_kb) / p.split_k);
+        j.kb1 = static_cast<int>((static_cast<int64_t>(split + 1) * p.num_kb) / p.split_k);
+        j.split = split;
+        j.tile = tile;
+    } else {
+        // binary search: group_prefix[g] <= w < group_prefix[g+1]
+        int lo = 0, hi = p.group_count - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (p.group_prefix[mid] <= w) lo = mid; else hi = mid - 1;
+        }
+        const TcGroupEntry& e = p.group[lo];
+        const int64_t t = w - p.group_prefix[lo];
+        const int in = static_cast<int>(t / e.tiles_m);
+        const int jm = static_cast<int>(t % e.tiles_m);
+        j.tmN = &e.tmN;
+        j.tmM = &e.tmM;
+        j.tmN_lo = &e.tmN;
+        j.tmM_lo = &e.tmM;
+        j.D = e.D;
+        j.C = e.C;
+        j.ldd = e.ldd;
+        j.ldc = e.ldc;
+        j.M = e.M;
+        j.N = e.N;
+        j.alpha = e.alpha;
+        j.beta = e.beta;
+        j.b = 0;
+        j.n0 = in * kTcTileN;
+        j.m0 = jm * p.bm;
+        j.kb0 = 0;
+        j.kb1 = (e.K + p.kb_elems - 1) / p.kb_elems;
+        j.split = 0;
+        j.tile = w;
+    }
+}
+
+__device__ __forceinline__ void record_error(const TcKernelParams& p, volatile int* abort_flag, int code)
+{
+    *abort_flag = 1;
+    atomicOr(p.err, code);
+}
+
+// ---- output conversion ------------------------------------------------------------------------------
+template <typename TD> struct Out;
+template <> struct Out<float> {
+    __device__ static __forceinline__ float load(const void* base, int64_t idx)
+    { return __ldg(static_cast<const float*>(base) + idx); }
+    __device__ static __forceinline__ void store(void* base, int64_t idx, float v, int)
+    { static_cast<float*>(base)[idx] = v; }
+    static constexpr int kBytes = 4;
+};
+template <> struct Out<__half> {
+    __device__ static __forceinline__ float load(const void* base, int64_t idx)
+    { return __half2float(static_cast<const __half*>(base)[idx]); }
+    __device__ static __forceinline__ void store(void* base, int64_t idx, float v, int)
+    { static_cast<__half*>(base)[idx] = __float2half_rn(v); }
+    static constexpr int kBytes = 2;
+};
+template <> struct Out<__nv_bfloat16> {
+    __device__ static __forceinline__ float load(const void* base, int64_t idx)
+    { return __bfloat162float(static_cast<const __nv_bfloat16*>(base)[idx]); }
+    __device__ static __forceinline__ void store(void* base, int64_t idx, float v, int trunc)
+    {
+        if (trunc) static_cast<uint16_t*>(base)[idx] = static_cast<uint16_t>(__float_as_uint(v) >> 16);
+        else static_cast<__nv_bfloat16*>(base)[idx] = __float2bfloat16_rn(v);
+    }
+    static constexpr int kBytes = 2;
+};
+
+__device__ __forceinline__ uint32_t pack2(float a, float b, int is_half, int trunc)
+{
+    if (is_half) {
+        __half2 h = __floats2half2_rn(a, b);
+        return *reinterpret_cast<uint32_t*>(&h);
+    }
+    if (trunc) return (__float_as_uint(a) >> 16) | (__float_as_uint(b) & 0xffff0000u);
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+
+__device__ __forceinline__ void unpack2(uint32_t w, int is_half, float& a, float& b)
+{
+    if (is_half) {
+        __half2 h = *reinterpret_cast<__half2*>(&w);
+        float2 f = __half22float2(h);
+        a = f.x;
+        b = f.y;
+    } else {
+        a = __uint_as_float(w << 16);
+        b = __uint_as_float(w & 0xffff0000u);
+    }
+}
+
+// Finish 32 consecutive outputs m..m+31 of column n: v = alpha*acc + beta*C, convert, store.
+template <typename TD>
+__device__ __forceinline__ void store_chunk(const TileJob& j, int64_t base_c, int64_t base_d, int m, float (&acc)[32],
+                                           int trunc)
+{
+    const bool full = (m + 32 <= j.M);
+    const bool use_c = (j.beta != 0.0f) && (j.C != nullptr);
+    char* dptr = static_cast<char*>(j.D) + (base_d + m) * Out<TD>::kBytes;
+    const char* cptr = use_c ? static_cast<const char*>(j.C) + (base_c + m) * Out<TD>::kBytes : nullptr;
+    const bool vec = full && ((reinterpret_cast<uintptr_t>(dptr) & 15) == 0) &&
+                     (!use_c || (reinterpret_cast<uintptr_t>(cptr) & 15) == 0);
+    if (vec) {
+        if constexpr (sizeof(TD) == 4) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                float4 c4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (use_c) c4 = __ldg(reinterpret_cast<const float4*>(cptr) + q);
+                float4 o;
+                if (use_c) {
+                    o.x = fmaf(j.alpha, acc[4 * q + 0], j.beta * c4.x);
+                    o.y = fmaf(j.alpha, acc[4 * q + 1], j.beta * c4.y);
+                    o.z = fmaf(j.alpha, acc[4 * q + 2], j.beta * c4.z);
+                    o.w = fmaf(j.alpha, acc[4 * q + 3], j.beta * c4.w);
+                } else {
+                    o.x = j.alpha * acc[4 * q + 0];
+                    o.y = j.alpha * acc[4 * q + 1];
+                    o.z = j.alpha * acc[4 * q + 2];
+                    o.w = j.alpha * acc[4 * q + 3];
+                }
+                reinterpret_cast<float4*>(dptr)[q] = o;
+            }
+        } else {
+            constexpr int is_half = std::is_same<TD, __half>::value ? 1 : 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                uint4 cw = make_uint4(0, 0, 0, 0);
+                if (use_c) cw = __ldg(reinterpret_cast<const uint4*>(cptr) + q);
+                uint32_t cws[4] = {cw.x, cw.y, cw.z, cw.w};
+                uint32_t ow[4];
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    float c0 = 0.f, c1 = 0.f;
+                    if (use_c) unpack2(cws[h], is_half, c0, c1);
+                    const float a0 = acc[8 * q + 2 * h], a1 = acc[8 * q + 2 * h + 1];
+                    const float o0 = use_c ? fmaf(j.alpha, a0, j.beta * c0) : j.alpha * a0;
+                    const float o1 = use_c ? fmaf(j.alpha, a1, j.beta * c1) : j.alpha * a1;
+                    ow[h] = pack2(o0, o1, is_half, trunc);
+                }
+                reinterpret_cast<uint4*>(dptr)[q] = make_uint4(ow[0], ow[1], ow[2], ow[3]);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+            if (m + i < j.M) {
+                float o;
+                if (use_c) o = fmaf(j.alpha, acc[i], j.beta * Out<TD>::load(j.C, base_c + m + i));
+                else o = j.alpha * acc[i];
+                Out<TD>::store(j.D, base_d + m + i, o, trunc);
+            }
+        }
+    }
+}
+
+template <int KIND, typename TD>
+__global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_constant__ TcKernelParams p)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const uint32_t tileN_bytes = kTcTileN * kTcRowBytes;
+    const uint32_t stage_bytes = tileN_bytes + static_cast<uint32_t>(p.bm) * kTcRowBytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(p.stages) * stage_bytes);
+    uint64_t* empty = full + kTcMaxStages;
+    uint64_t* tfull = empty + kTcMaxStages;
+    uint64_t* tempty = tfull + 2;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    volatile int* last_flag = abort_flag + 1;
+
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const uint32_t tmem_cols = (2 * p.bm <= 128) ? 128u : (2 * p.bm <= 256 ? 256u : 512u);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < p.stages; ++s) {
+            ptx::mbar_init(&full[s], 1);
+            ptx::mbar_init(&empty[s], 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            ptx::mbar_init(&tfull[a], 1);
+            ptx::mbar_init(&tempty[a], 128);
+        }
+        *abort_flag = 0;
+        *last_flag = 0;
+        ptx::fence_mbar_init();
+        ptx::fence_proxy_async_smem();
+    }
+    if (warp == 1) {
+        ptx::tmem_alloc(tmem_slot, tmem_cols);
+        ptx::tmem_relinquish();
+    }
+    if (warp == 0 && lane == 0 && p.group == nullptr) {
+        ptx::prefetch_tmap(&p.tmN);
+        ptx::prefetch_tmap(&p.tmM);
+        if (p.x3) {
+            ptx::prefetch_tmap(&p.tmN_lo);
+            ptx::prefetch_tmap(&p.tmM_lo);
+        }
+    }
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+    const int nvirt = p.x3 ? 3 : 1;
+    const uint64_t tlim = p.timeout_ns;
+
+    if (warp == 0) {
+        // ------------------------------------------------------------------ TMA producer
+        if (lane == 0) {
+            uint32_t stage = 0, phase = 0;
+            const int W = kTcRowBytes / (KIND == 0 ? 2 : 1);   // elements per 128-byte row
+            bool ok = true;
+            for (int64_t w = blockIdx.x; w < p.total_work && ok; w += gridDim.x) {
+                TileJob j;
+                get_job(p, w, j);
+                for (int kb = j.kb0; kb < j.kb1 && ok; ++kb) {
+                    for (int v = 0; v < nvirt; ++v) {
+                        if (!ptx::mbar_wait(&empty[stage], phase ^ 1u, tlim, abort_flag)) {
+                            record_error(p, abort_flag, 1);
+                            ok = false;
+                            break;
+                        }
+                        uint8_t* sN = smem + static_cast<size_t>(stage) * stage_bytes;
+                        uint8_t* sM = sN + tileN_bytes;
+                        // bf16x3 order per k-block: (B_lo, A_hi), (B_hi, A_lo), (B_hi, A_hi)
+                        const void* mapN = (p.x3 && v == 0) ? j.tmN_lo : j.tmN;
+                        const void* mapM = (p.x3 && v == 1) ? j.tmM_lo : j.tmM;
+                        ptx::mbar_arrive_expect_tx(&full[stage], stage_bytes);
+                        const int k0 = kb * W;
+                        if (!p.n_mn_major) {
+                            ptx::tma_load_3d(sN, mapN, &full[stage], k0, j.n0, j.b);
+                        } else {
+                            for (int c = 0; c < kTcTileN / W; ++c)
+                                ptx::tma_load_3d(sN + c * W * kTcRowBytes, mapN, &full[stage], j.n0 + c * W, k0, j.b);
+                        }
+                        if (!p.m_mn_major) {
+                            ptx::tma_load_3d(sM, mapM, &full[stage], k0, j.m0, j.b);
+                        } else {
+                            for (int c = 0; c < p.bm / W; ++c)
+                                ptx::tma_load_3d(sM + c * W * kTcRowBytes, mapM, &full[stage], j.m0 + c * W, k0, j.b);
+                        }
+                        if (++stage == static_cast<uint32_t>(p.stages)) {
+                            stage = 0;
+                            phase ^= 1u;
+                        }
+                    }
+                }
+            }
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            uint32_t stage = 0, phase = 0, acc = 0, acc_phase = 0;
+            bool ok = true;
+            for (int64_t w = blockIdx.x; w < p.total_work && ok; w += gridDim.x) {
+                TileJob j;
+                get_job(p, w, j);
+                if (!ptx::mbar_wait(&tempty[acc], acc_phase ^ 1u, tlim, abort_flag)) {
+                    record_error(p, abort_flag, 2);
+                    break;
+                }
+                ptx::tc_fence_after();
+                const uint32_t d_tmem = tmem_base + acc * static_cast<uint32_t>(p.bm);
+                const int nblk = (j.kb1 - j.kb0) * nvirt;
+                for (int i = 0; i < nblk; ++i) {
+                    if (!ptx::mbar_wait(&full[stage], phase, tlim, abort_flag)) {
+                        record_error(p, abort_flag, 4);
+                        ok = false;
+                        break;
+                    }
+                    ptx::tc_fence_after();
+                    const uint32_t sN = ptx::smem_u32(smem + static_cast<size_t>(stage) * stage_bytes);
+                    const uint32_t sM = sN + tileN_bytes;
+#pragma unroll
+                    for (int ks = 0; ks < 4; ++ks) {
+                        const uint64_t adesc = ptx::sdesc_sw128(sN + ks * p.n_kstep, p.n_lbo, 1024);
+                        const uint64_t bdesc = ptx::sdesc_sw128(sM + ks * p.m_kstep, p.m_lbo, 1024);
+                        const uint32_t accumulate = (i > 0 || ks > 0) ? 1u : 0u;
+                        if (KIND == 0) ptx::mma_f16(d_tmem, adesc, bdesc, p.idesc, accumulate);
+                        else ptx::mma_f8(d_tmem, adesc, bdesc, p.idesc, accumulate);
+                    }
+                    ptx::mma_commit(&empty[stage]);
+                    if (++stage == static_cast<uint32_t>(p.stages)) {
+                        stage = 0;
+                        phase ^= 1u;
+                    }
+                }
+                if (!ok) break;
+                ptx::mma_commit(&tfull[acc]);
+                acc ^= 1u;
+                if (acc == 0) acc_phase ^= 1u;
+            }
+        }
+    } else {
+        // ------------------------------------------------------------------ epilogue (4 warps)
+        // All four warps run the same loop and, in split-k mode, the same named barriers: after a
+        // timed-out wait a warp keeps the control flow and only skips the work, so no warp can be
+        // left waiting at bar.sync 1 for one that gave up.
+        const int quarter = warp & 3;             // TMEM lanes 32*quarter .. +31
+        const int row = quarter * 32 + lane;      // tile row = problem n offset
+        const int et = threadIdx.x - 64;          // 0..127
+        uint32_t acc = 0, acc_phase = 0;
+        const int chunks = p.bm / 32;
+        bool ok = true;
+        for (int64_t w = blockIdx.x; w < p.total_work; w += gridDim.x) {
+            TileJob j;
+            get_job(p, w, j);
+            bool got = ok && ptx::mbar_wait(&tfull[acc], acc_phase, tlim, abort_flag);
+            got = __all_sync(0xffffffffu, got);
+            if (ok && !got) {
+                if (lane == 0) record_error(p, abort_flag, 8);
+                ok = false;
+            }
+            const int n = j.n0 + row;
+            const bool row_ok = n < j.N;
+            const int64_t base_d = static_cast<int64_t>(j.b) * p.stride_d + static_cast<int64_t>(n) * j.ldd;
+            const int64_t base_c = static_cast<int64_t>(j.b) * p.stride_c + static_cast<int64_t>(n) * j.ldc;
+            const uint32_t tbase = tmem_base + (static_cast<uint32_t>(quarter * 32) << 16) + acc * p.bm;
+            if (ok) ptx::tc_fence_after();
+            if (p.split_k == 1) {
+                for (int c = 0; c < chunks && ok; ++c) {
+                    uint32_t r[32];
+                    __syncwarp();
+                    ptx::tmem_ld32(tbase + c * 32, r);
+                    if (c == chunks - 1) {
+                        ptx::tc_fence_before();
+                        ptx::mbar_arrive(&tempty[acc]);
+                    }
+                    const int m = j.m0 + c * 32;
+                    if (row_ok && m < j.M) {
+                        float v[32];
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+                        store_chunk<TD>(j, base_c, base_d, m, v, p.out_trunc);
+                    }
+                }
+            } else {
+                // split-k: park this split's partial tile, thread-private layout [chunk][row][32]
+                float* slab = p.ws + (static_cast<size_t>(j.tile) * p.split_k + j.split) *
+                                         (static_cast<size_t>(kTcTileN) * p.bm);
+                for (int c = 0; c < chunks && ok; ++c) {
+                    uint32_t r[32];
+                    __syncwarp();
+                    ptx::tmem_ld32(tbase + c * 32, r);
+                    if (c == chunks - 1) {
+                        ptx::tc_fence_before();
+                        ptx::mbar_arrive(&tempty[acc]);
+                    }
+                    float4* dst = reinterpret_cast<float4*>(slab + (static_cast<size_t>(c) * kTcTileN + row) * 32);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        __stcg(dst + q, make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
+                                                    __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3])));
+                }
+                __threadfence();
+                asm volatile("bar.sync 1, 128;" ::: "memory");
+                if (et == 0) {
+                    int last = 0;
+                    if (ok) last = (atomicAdd(p.counters + j.tile, 1) == p.split_k - 1) ? 1 : 0;
+                    *last_flag = last;
+                }
+                asm volatile("bar.sync 1, 128;" ::: "memory");
+                const int is_last = *last_flag;
+                if (is_last && ok) {
+                    __threadfence();
+                    for (int c = 0; c < chunks; ++c) {
+                        float v[32];
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) v[i] = 0.f;
+                        for (int s = 0; s < p.split_k; ++s) {
+                            const float4* src = reinterpret_cast<const float4*>(
+                                p.ws + (static_cast<size_t>(j.tile) * p.split_k + s) * (static_cast<size_t>(kTcTileN) * p.bm) +
+                                (static_cast<size_t>(c) * kTcTileN + row) * 32);
+#pragma unroll
+                            for (int q = 0; q < 8; ++q) {
+                                const float4 f = __ldcg(src + q);
+                                v[4 * q] += f.x;
+                                v[4 * q + 1] += f.y;
+                                v[4 * q + 2] += f.z;
+                                v[4 * q + 3] += f.w;
+                            }
+                        }
+                        const int m = j.m0 + c * 32;
+                        if (row_ok && m < j.M) store_chunk<TD>(j, base_c, base_d, m, v, p.out_trunc);
+                    }
+                    if (et == 0) p.counters[j.tile] = 0;   // ready for the next launch
+                }
+                asm volatile("bar.sync 1, 128;" ::: "memory");   // last_flag is reused next tile
+            }
+            acc ^= 1u;
+            if (acc == 0) acc_phase ^= 1u;
+        }
+    }
+
+    ptx::tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        ptx::tc_fence_after();
+        ptx::tmem_dealloc(tmem_base, tmem_cols);
+    }
+}
+
+// ---- host side ------------------------------------------------------------------------------------
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn get_encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(ptr);
+    });
+    return fn;
+}
+
+template <int KIND, typename TD>
+tl_status launch_kernel(const TcKernelParams& kp, int grid, size_t smem, cudaStream_t stream)
+{
+    auto kern = tc_gemm_kernel<KIND, TD>;
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(once, [&] {
+        attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    });
+    if (attr_err != cudaSuccess) return cuda_fail(attr_err, "cudaFuncSetAttribute(tc_gemm_kernel)");
+    kern<<<grid, kTcThreads, smem, stream>>>(kp);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "tc_gemm_kernel launch");
+    return TL_SUCCESS;
+}
+
+tl_status dispatch(int in_dtype, int out_dtype, const TcKernelParams& kp, int grid, size_t smem, cudaStream_t s)
+{
+    const int kind = (in_dtype == TL_DTYPE_FP8_E4M3) ? 1 : 0;
+    if (kind == 0) {
+        if (out_dtype == TL_DTYPE_FP32) return launch_kernel<0, float>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_FP16) return launch_kernel<0, __half>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_BF16) return launch_kernel<0, __nv_bfloat16>(kp, grid, smem, s);
+    } else {
+        if (out_dtype == TL_DTYPE_FP32) return launch_kernel<1, float>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_FP16) return launch_kernel<1, __half>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_BF16) return launch_kernel<1, __nv_bfloat16>(kp, grid, smem, s);
+    }
+    return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel: unsupported output type");
+}
+
+uint32_t make_idesc(int in_dtype, int n_mn_major, int m_mn_major, int bm)
+{
+    uint32_t d = 1u << 4;                                  // accumulator F32
+    uint32_t t = (in_dtype == TL_DTYPE_BF16) ? 1u : 0u;    // kind::f16: 0 F16, 1 BF16; f8f6f4: 0 E4M3
+    d |= t << 7;                                           // A (problem B^T) type
+    d |= t << 10;                                          // B (problem A) type
+    d |= static_cast<uint32_t>(n_mn_major & 1) << 15;      // A major: 0 K, 1 MN
+    d |= static_cast<uint32_t>(m_mn_major & 1) << 16;      // B major
+    d |= static_cast<uint32_t>(bm >> 3) << 17;             // N >> 3
+    d |= static_cast<uint32_t>(kTcTileN >> 4) << 24;       // M >> 4
+    return d;
+}
+
+void desc_params(int in_dtype, int mn_major, uint32_t& lbo, uint32_t& kstep)
+{
+    const int es = dtype_bytes(in_dtype);
+    const int W = kTcRowBytes / es;          // elements per 128-byte row == depth_u
+    const int umma_k = 32 / es;              // 16 for 16-bit, 32 for fp8
+    if (!mn_major) {
+        lbo = 16;                            // unused for swizzled K-major
+        kstep = umma_k * es;                 // 32 bytes along the swizzled row
+    } else {
+        lbo = static_cast<uint32_t>(W) * kTcRowBytes;   // next MN chunk of W elements
+        kstep = umma_k * kTcRowBytes;                    // umma_k rows of 128 bytes
+    }
+}
+
+}  // namespace
+
+size_t tc_smem_bytes(int bm, int stages)
+{
+    // ring + 1024 bytes to align the ring + barriers/flags (with margin)
+    return static_cast<size_t>(stages) * (kTcTileN * kTcRowBytes + bm * kTcRowBytes) + 1024 + 512;
+}
+
+int tc_tmem_cols(int bm) { return (2 * bm <= 128) ? 128 : (2 * bm <= 256 ? 256 : 512); }
+
+tl_status tc_encode_operand(CUtensorMap* tm, int in_dtype, const TcOperand& op, int64_t K, int64_t batch,
+                            int box_rows)
+{
+    EncodeTiledFn enc = get_encode_fn();
+    if (!enc) return fail(TL_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
+    const int es = dtype_bytes(in_dtype);
+    const int W = kTcRowBytes / es;
+    CUtensorMapDataType dt = in_dtype == TL_DTYPE_BF16   ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                             : in_dtype == TL_DTYPE_FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                         : CU_TENSOR_MAP_DATA_TYPE_UINT8;
+    cuuint64_t dims[3];
+    cuuint64_t strides[2];
+    cuuint32_t box[3];
+    cuuint32_t estr[3] = {1, 1, 1};
+    if (!op.mn_major) {
+        dims[0] = static_cast<cuuint64_t>(K);
+        dims[1] = static_cast<cuuint64_t>(op.rows);
+        box[0] = W;
+        box[1] = box_rows;
+    } else {
+        dims[0] = static_cast<cuuint64_t>(op.rows);
+        dims[1] = static_cast<cuuint64_t>(K);
+        box[0] = W;
+        box[1] = W;
+    }
+    dims[2] = static_cast<cuuint64_t>(batch);
+    box[2] = 1;
+    strides[0] = static_cast<cuuint64_t>(op.ld) * es;
+    cuuint64_t bstride = static_cast<cuuint64_t>(op.batch_stride) * es;
+    if (batch <= 1) bstride = ((strides[0] * dims[1]) + 15) & ~cuuint64_t(15);
+    strides[1] = bstride;
+    CUresult r = enc(tm, dt, 3, const_cast<void*>(op.ptr), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        char buf[256];
+        snprintf(buf, sizeof(buf),
+                 "cuTensorMapEncodeTiled failed (%d): dims {%llu,%llu,%llu} strides {%llu,%llu} box {%u,%u}",
+                 static_cast<int>(r), (unsigned long long)dims[0], (unsigned long long)dims[1],
+                 (unsigned long long)dims[2], (unsigned long long)strides[0], (unsigned long long)strides[1], box[0],
+                 box[1]);
+        return fail(TL_ERR_INVALID_ARG, buf);
+    }
+    return TL_SUCCESS;
+}
+
+tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launches)
+{
+    TcKernelParams kp;
+    memset(&kp, 0, sizeof(kp));
+    tl_status st;
+    if ((st = tc_encode_operand(&kp.tmN, L.in_dtype, L.opN, L.K, L.batch, kTcTileN)) != TL_SUCCESS) return st;
+    if ((st = tc_encode_operand(&kp.tmM, L.in_dtype, L.opM, L.K, L.batch, L.bm)) != TL_SUCCESS) return st;
+    if (L.x3) {
+        if ((st = tc_encode_operand(&kp.tmN_lo, L.in_dtype, L.opN_lo, L.K, L.batch, kTcTileN)) != TL_SUCCESS) return st;
+        if ((st = tc_encode_operand(&kp.tmM_lo, L.in_dtype, L.opM_lo, L.K, L.batch, L.bm)) != TL_SUCCESS) return st;
+    }
+    const int W = kTcRowBytes / dtype_bytes(L.in_dtype);
+    kp.group = nullptr;
+    kp.D = L.D;
+    kp.C = L.C;
+    kp.ldd = L.ldd;
+    kp.ldc = L.ldc;
+    kp.stride_d = L.stride_d;
+    kp.stride_c = L.stride_c;
+    kp.M = static_cast<int>(L.M);
+    kp.N = static_cast<int>(L.N);
+    kp.K = static_cast<int>(L.K);
+    kp.batch = static_cast<int>(L.batch);
+    kp.alpha = L.alpha;
+    kp.beta = L.beta;
+    kp.bm = L.bm;
+    kp.stages = L.stages;
+    kp.split_k = L.split_k;
+    kp.raster = L.raster;
+    kp.x3 = L.x3;
+    kp.tiles_m = static_cast<int>((L.M + L.bm - 1) / L.bm);
+    kp.tiles_n = static_cast<int>((L.N + kTcTileN - 1) / kTcTileN);
+    kp.num_kb = static_cast<int>((L.K + W - 1) / W);
+    kp.kb_elems = W;
+    kp.total_work = static_cast<int64_t>(kp.tiles_m) * kp.tiles_n * L.batch * L.split_k;
+    kp.n_mn_major = L.opN.mn_major;
+    kp.m_mn_major = L.opM.mn_major;
+    kp.idesc = make_idesc(L.in_dtype, kp.n_mn_major, kp.m_mn_major, L.bm);
+    desc_params(L.in_dtype, kp.n_mn_major, kp.n_lbo, kp.n_kstep);
+    desc_params(L.in_dtype, kp.m_mn_major, kp.m_lbo, kp.m_kstep);
+    kp.out_trunc = L.out_trunc;
+    kp.ws = L.workspace;
+    kp.counters = L.counters;
+    kp.err = L.err;
+    kp.timeout_ns = L.timeout_ns;
+    int grid = L.ctas > 0 ? L.ctas : L.sm_count;
+    if (grid > kp.total_work) grid = static_cast<int>(kp.total_work);
+    if (grid < 1) grid = 1;
+    const size_t smem = tc_smem_bytes(L.bm, L.stages);
+    st = dispatch(L.in_dtype, L.out_dtype, kp, grid, smem, stream);
+    if (st == TL_SUCCESS && launches) ++*launches;
+    return st;
+}
+
+tl_status tc_grouped_launch(const TcGroupLaunch& G, cudaStream_t stream, int64_t* launches)
+{
+    TcKernelParams kp;
+    memset(&kp, 0, sizeof(kp));
+    kp.group = G.d_entries;
+    kp.group_prefix = G.d_tile_prefix;
+    kp.group_count = G.count;
+    kp.bm = G.bm;
+    kp.stages = G.stages;
+    kp.split_k = 1;
+    kp.x3 = 0;
+    kp.total_work = G.total_tiles;
+    kp.kb_elems = kTcRowBytes / dtype_bytes(G.in_dtype);
+    kp.stride_c = 0;
+    kp.stride_d = 0;
+    kp.n_mn_major = G.n_mn_major;
+    kp.m_mn_major = G.m_mn_major;
+    kp.idesc = make_idesc(G.in_dtype, G.n_mn_major, G.m_mn_major, G.bm);
+    desc_params(G.in_dtype, G.n_mn_major, kp.n_lbo, kp.n_kstep);
+    desc_params(G.in_dtype, G.m_mn_major, kp.m_lbo, kp.m_kstep);
+    kp.out_trunc = G.out_trunc;
+    kp.err = G.err;
+    kp.timeout_ns = G.timeout_ns;
+    int grid = G.ctas > 0 ? G.ctas : G.sm_count;
+    if (grid > G.total_tiles) grid = static_cast<int>(G.total_tiles);
+    if (grid < 1) grid = 1;
+    const size_t smem = tc_smem_bytes(G.bm, G.stages);
+    tl_status st = dispatch(G.in_dtype, G.out_dtype, kp, grid, smem, stream);
+    if (st == TL_SUCCESS && launches) ++*launches;
+    return st;
+}
+
+}  // namespace tl

@@ -1,0 +1,1212 @@
+// tl_api.cpp -- the C ABI (include/tensilelite.h) over the CUDA runtime.
+//
+// Host-side counterpart of TensileLite's L2/L3 harness: problem validation and solution choice
+// (GemmMfmaSolver / GemmMfmaAsmSolution::generateKernel, src/gemmMfma.cpp:20-185), legality
+// (checkKernelParameters, src/gemmMfmaKernelWriter.h:321-405), launch (StreamHip::Launch,
+// ff_gpu_src/ff_hip_runtime.cpp:278-320) and the runtime's buffer calls (inc/ff_gpu.h:240-333).
+// Unlike the reference, nothing here exits the process, launches are asynchronous on the caller's
+// stream, and the runtime is a per-device handle rather than a global singleton.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "tl_internal.h"
+
+struct tl_handle {
+    int device = 0;
+    int sm_count = 0;
+    int cc_major = 0, cc_minor = 0;
+    size_t smem_optin = 0;
+    char name[256] = {0};
+    int* d_err = nullptr;          // device error word
+    double* d_norms = nullptr;     // error-norm scratch (3 doubles)
+    float* d_amax = nullptr;       // fp8 amax scratch
+    void* ws = nullptr;            // workspace: split-k partials, bf16x3 operands
+    size_t ws_bytes = 0;
+    int* counters = nullptr;       // split-k arrival counters (self-resetting)
+    size_t counters_len = 0;
+    int64_t launches = 0;
+    uint64_t timeout_ns = 4000000000ull;
+    std::map<std::string, tl_gemm_solution> tuned;
+    std::mutex mu;
+};
+
+struct tl_grouped_plan {
+    tl_handle* h = nullptr;
+    tl::TcGroupEntry* d_entries = nullptr;
+    int64_t* d_prefix = nullptr;
+    tl::TcGroupLaunch launch{};
+    tl_gemm_solution sol{};
+    double flops = 0.0;
+};
+
+struct tl_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+struct tl_timer {
+    cudaEvent_t start = nullptr, stop = nullptr;
+};
+
+namespace tl {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+tl_status fail(tl_status st, const std::string& msg)
+{
+    g_last_error = msg;
+    return st;
+}
+
+tl_status cuda_fail(cudaError_t e, const char* what)
+{
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    g_last_error = m;
+    return TL_ERR_CUDA;
+}
+
+namespace {
+
+cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+std::string dims_str(const tl_gemm_problem& p)
+{
+    char buf[200];
+    snprintf(buf, sizeof(buf), "m=%lld n=%lld k=%lld batch=%lld", (long long)p.m, (long long)p.n, (long long)p.k,
+             (long long)p.batch);
+    return buf;
+}
+
+// Basic validation shared by every path (sizes, leading dimensions, dtypes).
+tl_status validate(const tl_gemm_problem* p)
+{
+    if (!p) return fail(TL_ERR_INVALID_ARG, "problem is NULL");
+    if (p->m < 0 || p->n < 0 || p->k < 0 || p->batch < 1)
+        return fail(TL_ERR_INVALID_ARG, "negative size or batch < 1: " + dims_str(*p));
+    if (p->m > 0x7fffffffLL || p->n > 0x7fffffffLL || p->k > 0x7fffffffLL || p->batch > 65535)
+        return fail(TL_ERR_UNSUPPORTED, "size beyond 2^31-1 (or batch > 65535): " + dims_str(*p));
+    if (dtype_bytes(p->dtype_a) == 0 || dtype_bytes(p->dtype_d) == 0)
+        return fail(TL_ERR_INVALID_ARG, "unknown dtype");
+    if (p->dtype_a != p->dtype_b) return fail(TL_ERR_UNSUPPORTED, "dtype_a != dtype_b");
+    if (p->dtype_c != p->dtype_d) return fail(TL_ERR_UNSUPPORTED, "dtype_c != dtype_d");
+    if (p->dtype_d == TL_DTYPE_FP8_E4M3) return fail(TL_ERR_UNSUPPORTED, "fp8 output is not supported");
+    if (p->dtype_a == TL_DTYPE_FP32 && p->dtype_d != TL_DTYPE_FP32)
+        return fail(TL_ERR_UNSUPPORTED, "fp32 inputs need an fp32 output");
+    if ((p->trans_a != TL_OP_N && p->trans_a != TL_OP_T) || (p->trans_b != TL_OP_N && p->trans_b != TL_OP_T))
+        return fail(TL_ERR_INVALID_ARG, "trans flags must be TL_OP_N or TL_OP_T");
+    const int64_t a_rows = p->trans_a ? p->k : p->m;   // stored rows (leading dimension extent)
+    const int64_t b_rows = p->trans_b ? p->n : p->k;
+    if (p->lda < std::max<int64_t>(1, a_rows)) return fail(TL_ERR_INVALID_ARG, "lda smaller than op(A) storage rows");
+    if (p->ldb < std::max<int64_t>(1, b_rows)) return fail(TL_ERR_INVALID_ARG, "ldb smaller than op(B) storage rows");
+    if (p->ldd < std::max<int64_t>(1, p->m)) return fail(TL_ERR_INVALID_ARG, "ldd < m");
+    if (p->beta != 0.0f && p->ldc < std::max<int64_t>(1, p->m)) return fail(TL_ERR_INVALID_ARG, "ldc < m");
+    if (p->kernel < TL_KERNEL_AUTO || p->kernel > TL_KERNEL_BF16X3) return fail(TL_ERR_INVALID_ARG, "bad kernel id");
+    if (p->kernel == TL_KERNEL_BF16X3 && p->dtype_a != TL_DTYPE_FP32)
+        return fail(TL_ERR_UNSUPPORTED, "bf16x3 needs fp32 inputs");
+    if (p->kernel == TL_KERNEL_TCGEN05 && p->dtype_a == TL_DTYPE_FP32)
+        return fail(TL_ERR_UNSUPPORTED, "the tcgen05 kernel takes fp16/bf16/fp8 inputs (use BF16X3 for fp32)");
+    if (p->out_rounding != TL_ROUND_RNE && p->out_rounding != TL_ROUND_TRUNCATE)
+        return fail(TL_ERR_INVALID_ARG, "bad out_rounding");
+    return TL_SUCCESS;
+}
+
+float scale_of(float s) { return s == 0.0f ? 1.0f : s; }
+
+int tc_in_dtype(const tl_gemm_problem& p) { return p.dtype_a == TL_DTYPE_FP32 ? TL_DTYPE_BF16 : p.dtype_a; }
+
+int row_elems(int in_dtype) { return kTcRowBytes / dtype_bytes(in_dtype); }
+
+// Can TMA describe the operands as given?  (strides multiples of 16 bytes, 16-byte aligned bases)
+bool tma_ok(const tl_gemm_problem& p, const void* A, const void* B, std::string* why)
+{
+    const int es = dtype_bytes(p.dtype_a);
+    auto bad = [&](const char* w) { if (why) *why = w; return false; };
+    if (p.kernel == TL_KERNEL_BF16X3) return true;   // operands are re-laid into the workspace
+    if (!aligned16(A) || !aligned16(B)) return bad("A/B not 16-byte aligned");
+    if ((p.lda * es) % 16 || (p.ldb * es) % 16) return bad("lda/ldb not a multiple of 16 bytes");
+    if (p.batch > 1 && (((p.stride_a * es) % 16) || ((p.stride_b * es) % 16)))
+        return bad("batch strides of A/B not multiples of 16 bytes");
+    return true;
+}
+
+int resolve_kernel(const tl_gemm_problem& p)
+{
+    if (p.kernel != TL_KERNEL_AUTO) return p.kernel;
+    return p.dtype_a == TL_DTYPE_FP32 ? TL_KERNEL_SIMT : TL_KERNEL_TCGEN05;
+}
+
+int max_stages(int bm, size_t smem_optin)
+{
+    int s = kTcMaxStages;
+    while (s > 2 && tc_smem_bytes(bm, s) > smem_optin) --s;
+    return s;
+}
+
+void simt_solution(tl_gemm_solution* s)
+{
+    memset(s, 0, sizeof(*s));
+    s->kernel = TL_KERNEL_SIMT;
+    s->macro_tile0 = 128;
+    s->macro_tile1 = 128;
+    s->depth_u = 8;
+    s->stages = 2;
+    s->wave_tile0 = 8;
+    s->wave_tile1 = 8;
+    s->split_k = 1;
+}
+
+bool m_mn_major(const tl_gemm_problem& p) { return p.trans_a == TL_OP_N; }   // A[m + k*lda]
+bool n_mn_major(const tl_gemm_problem& p) { return p.trans_b == TL_OP_T; }   // B[n + k*ldb]
+
+void tc_heuristic(const tl_handle* h, const tl_gemm_problem& p, int kernel, tl_gemm_solution* s)
+{
+    memset(s, 0, sizeof(*s));
+    s->kernel = kernel;
+    const int in = (kernel == TL_KERNEL_BF16X3) ? TL_DTYPE_BF16 : p.dtype_a;
+    const int W = row_elems(in);
+    const bool mmn = (kernel == TL_KERNEL_BF16X3) ? false : m_mn_major(p);
+    const int64_t tiles_n = (p.n + kTcTileN - 1) / kTcTileN;
+    const int64_t num_kb = (p.k + W - 1) / W;
+    int bm = 256;
+    const int cands[3] = {256, 128, 64};
+    for (int c : cands) {
+        if (mmn && c % W) continue;
+        bm = c;
+        const int64_t tiles = tiles_n * ((p.m + c - 1) / c) * p.batch;
+        if (tiles >= h->sm_count) break;
+        if (c == 64 || (mmn && c == W)) break;
+    }
+    if (mmn && bm % W) bm = 2 * W > 256 ? W : 2 * W;
+    const int64_t tiles = tiles_n * ((p.m + bm - 1) / bm) * p.batch;
+    int split = 1;
+    if (tiles < h->sm_count / 2 && num_kb >= 8) {
+        split = static_cast<int>(std::min<int64_t>(h->sm_count / std::max<int64_t>(1, tiles), num_kb / 4));
+        split = std::max(1, std::min(split, 16));
+    }
+    s->macro_tile0 = bm;
+    s->macro_tile1 = kTcTileN;
+    s->depth_u = W;
+    s->stages = max_stages(bm, h->smem_optin);
+    s->wave_tile0 = 0;
+    s->wave_tile1 = 0;
+    s->split_k = split;
+    s->raster = tiles_n > 8 ? 8 : 0;
+    s->ctas = 0;
+}
+
+tl_status check_tc_solution(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solution& s)
+{
+    const int in = (s.kernel == TL_KERNEL_BF16X3) ? TL_DTYPE_BF16 : p.dtype_a;
+    if (in != TL_DTYPE_FP16 && in != TL_DTYPE_BF16 && in != TL_DTYPE_FP8_E4M3)
+        return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel needs fp16, bf16 or fp8 operands");
+    const int W = row_elems(in);
+    if (s.macro_tile1 != kTcTileN) return fail(TL_ERR_UNSUPPORTED, "macro_tile1 (n) must be 128 for tcgen05");
+    const int bm = s.macro_tile0;
+    if (bm != 64 && bm != 128 && bm != 192 && bm != 256)
+        return fail(TL_ERR_UNSUPPORTED, "macro_tile0 (m) must be 64, 128, 192 or 256");
+    const bool mmn = (s.kernel == TL_KERNEL_BF16X3) ? false : m_mn_major(p);
+    if (mmn && bm % W) return fail(TL_ERR_UNSUPPORTED, "macro_tile0 must be a multiple of the 128-byte row for MN-major A");
+    if (s.depth_u != 0 && s.depth_u != W) return fail(TL_ERR_UNSUPPORTED, "depth_u is fixed to one 128-byte row");
+    if (s.stages < 2 || s.stages > kTcMaxStages) return fail(TL_ERR_UNSUPPORTED, "stages must be in [2, 8]");
+    if (tc_smem_bytes(bm, s.stages) > h->smem_optin) return fail(TL_ERR_UNSUPPORTED, "shared memory budget exceeded");
+    const int64_t num_kb = (p.k + W - 1) / W;
+    if (s.split_k < 1 || (num_kb > 0 && s.split_k > num_kb) || s.split_k > 64)
+        return fail(TL_ERR_UNSUPPORTED, "split_k must be in [1, min(64, k blocks)]");
+    if (s.raster < 0 || s.ctas < 0) return fail(TL_ERR_INVALID_ARG, "raster and ctas must be >= 0");
+    return TL_SUCCESS;
+}
+
+std::string problem_key(const tl_handle* h, const tl_gemm_problem& p)
+{
+    char buf[400];
+    snprintf(buf, sizeof(buf), "%s|sm%d%d|a%d|d%d|k%d|%c%c|%lld|%lld|%lld|%lld|%lld|%lld", h->name, h->cc_major,
+             h->cc_minor, p.dtype_a, p.dtype_d, p.kernel, p.trans_a ? 'T' : 'N', p.trans_b ? 'T' : 'N', (long long)p.m,
+             (long long)p.n, (long long)p.k, (long long)p.batch, (long long)p.lda, (long long)p.ldb);
+    for (char* c = buf; *c; ++c)
+        if (*c == '"' || *c == '\\') *c = '_';
+    return buf;
+}
+
+tl_status ensure_ws(tl_handle* h, size_t bytes)
+{
+    if (bytes <= h->ws_bytes) return TL_SUCCESS;
+    if (h->ws) {
+        cudaDeviceSynchronize();
+        cudaFree(h->ws);
+        h->ws = nullptr;
+        h->ws_bytes = 0;
+    }
+    size_t want = std::max<size_t>(bytes, 1 << 20);
+    cudaError_t e = cudaMalloc(&h->ws, want);
+    if (e != cudaSuccess) return fail(TL_ERR_ALLOC, "workspace allocation failed");
+    h->ws_bytes = want;
+    return TL_SUCCESS;
+}
+
+tl_status ensure_counters(tl_handle* h, size_t n)
+{
+    if (n <= h->counters_len) return TL_SUCCESS;
+    if (h->counters) {
+        cudaDeviceSynchronize();
+        cudaFree(h->counters);
+        h->counters = nullptr;
+        h->counters_len = 0;
+    }
+    size_t want = std::max<size_t>(n, 4096);
+    if (cudaMalloc(&h->counters, want * sizeof(int)) != cudaSuccess) return fail(TL_ERR_ALLOC, "counter allocation failed");
+    if (cudaMemset(h->counters, 0, want * sizeof(int)) != cudaSuccess) return fail(TL_ERR_CUDA, "counter memset failed");
+    h->counters_len = want;
+    return TL_SUCCESS;
+}
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Everything a GEMM launch needs once the solution is fixed; preparing allocates, enqueueing
+// only launches (so enqueue can be captured in a CUDA graph).
+struct Prepared {
+    tl_gemm_problem p;
+    tl_gemm_solution s;
+    int kernel;
+    void* D;
+    const void* C;
+    const void* A;
+    const void* B;
+    // bf16x3 operand copies in the workspace
+    uint16_t *a_hi = nullptr, *a_lo = nullptr, *b_hi = nullptr, *b_lo = nullptr;
+    int64_t a_span = 0, b_span = 0;
+    float* ws_partials = nullptr;
+};
+
+int64_t operand_span(int64_t ld, int64_t cols, int64_t batch, int64_t bstride, int64_t rows)
+{
+    if (rows == 0 || cols == 0) return 0;
+    return (batch - 1) * bstride + (cols - 1) * ld + rows;
+}
+
+tl_status prepare(tl_handle* h, const tl_gemm_problem* prob, const tl_gemm_solution* sol, void* D, const void* C,
+                  const void* A, const void* B, Prepared* out)
+{
+    tl_status st = validate(prob);
+    if (st != TL_SUCCESS) return st;
+    Prepared& P = *out;
+    P.p = *prob;
+    P.D = D; P.C = C; P.A = A; P.B = B;
+    const tl_gemm_problem& p = P.p;
+    if ((p.m && p.n) && !D) return fail(TL_ERR_INVALID_ARG, "D is NULL");
+    if (p.beta != 0.0f && !C && p.m && p.n) return fail(TL_ERR_INVALID_ARG, "C is NULL with beta != 0");
+    if (p.k > 0 && p.m > 0 && p.n > 0 && (!A || !B)) return fail(TL_ERR_INVALID_ARG, "A or B is NULL");
+
+    int kernel = resolve_kernel(p);
+    if (sol) {
+        P.s = *sol;
+        if (P.s.kernel == TL_KERNEL_AUTO) P.s.kernel = kernel;
+        kernel = P.s.kernel;
+        if (p.kernel != TL_KERNEL_AUTO && kernel != p.kernel)
+            return fail(TL_ERR_INVALID_ARG, "solution kernel differs from the problem's kernel request");
+    } else {
+        std::lock_guard<std::mutex> g(h->mu);
+        auto it = h->tuned.find(problem_key(h, p));
+        if (it != h->tuned.end()) {
+            P.s = it->second;
+            kernel = P.s.kernel;
+        } else if (kernel == TL_KERNEL_SIMT) {
+            simt_solution(&P.s);
+        } else {
+            tc_heuristic(h, p, kernel, &P.s);
+        }
+    }
+    // operands the TMA cannot describe fall back to the SIMT kernel when the caller left it to us
+    std::string why;
+    const bool has_work = p.m > 0 && p.n > 0 && p.k > 0;
+    if (kernel == TL_KERNEL_TCGEN05 && has_work && !tma_ok(p, A, B, &why)) {
+        if (p.kernel == TL_KERNEL_AUTO && !sol) {
+            kernel = TL_KERNEL_SIMT;
+            simt_solution(&P.s);
+        } else {
+            return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel: " + why);
+        }
+    }
+    P.kernel = kernel;
+    if (kernel == TL_KERNEL_SIMT) {
+        if (P.s.macro_tile0 != 128 || P.s.macro_tile1 != 128 || (P.s.depth_u && P.s.depth_u != 8) ||
+            (P.s.split_k > 1))
+            return fail(TL_ERR_UNSUPPORTED, "SIMT kernel supports macro tile 128x128, depth_u 8, split_k 1");
+        return TL_SUCCESS;
+    }
+    if (kernel == TL_KERNEL_TCGEN05 && p.dtype_a == TL_DTYPE_FP32)
+        return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel needs fp16/bf16/fp8 inputs");
+    if (kernel == TL_KERNEL_BF16X3 && p.dtype_a != TL_DTYPE_FP32)
+        return fail(TL_ERR_UNSUPPORTED, "bf16x3 needs fp32 inputs");
+    if ((st = check_tc_solution(h, p, P.s)) != TL_SUCCESS) return st;
+    if (p.m == 0 || p.n == 0 || p.k == 0) return TL_SUCCESS;
+
+    // workspace: [bf16x3 operands][split-k partials]
+    size_t need = 0;
+    size_t off_ahi = 0, off_alo = 0, off_bhi = 0, off_blo = 0, off_part = 0;
+    if (kernel == TL_KERNEL_BF16X3) {
+        const int64_t a_rows = p.trans_a ? p.k : p.m, a_cols = p.trans_a ? p.m : p.k;
+        const int64_t b_rows = p.trans_b ? p.n : p.k, b_cols = p.trans_b ? p.k : p.n;
+        P.a_span = operand_span(p.lda, a_cols, p.batch, p.stride_a, a_rows);
+        P.b_span = operand_span(p.ldb, b_cols, p.batch, p.stride_b, b_rows);
+        off_ahi = 0;
+        off_alo = align_up(off_ahi + P.a_span * 2, 256);
+        off_bhi = align_up(off_alo + P.a_span * 2, 256);
+        off_blo = align_up(off_bhi + P.b_span * 2, 256);
+        need = align_up(off_blo + P.b_span * 2, 256);
+    }
+    const int W = row_elems(tc_in_dtype(p));
+    (void)W;
+    const int64_t tiles = ((p.n + kTcTileN - 1) / kTcTileN) * ((p.m + P.s.macro_tile0 - 1) / P.s.macro_tile0) * p.batch;
+    if (P.s.split_k > 1) {
+        off_part = need;
+        need = off_part + static_cast<size_t>(tiles) * P.s.split_k * kTcTileN * P.s.macro_tile0 * sizeof(float);
+        if ((st = ensure_counters(h, static_cast<size_t>(tiles))) != TL_SUCCESS) return st;
+    }
+    if (need) {
+        if ((st = ensure_ws(h, need)) != TL_SUCCESS) return st;
+        char* base = static_cast<char*>(h->ws);
+        if (kernel == TL_KERNEL_BF16X3) {
+            P.a_hi = reinterpret_cast<uint16_t*>(base + off_ahi);
+            P.a_lo = reinterpret_cast<uint16_t*>(base + off_alo);
+            P.b_hi = reinterpret_cast<uint16_t*>(base + off_bhi);
+            P.b_lo = reinterpret_cast<uint16_t*>(base + off_blo);
+        }
+        if (P.s.split_k > 1) P.ws_partials = reinterpret_cast<float*>(base + off_part);
+    }
+    if (kernel == TL_KERNEL_BF16X3) {
+        // the split copies keep the caller's leading dimensions; TMA needs them 16-byte aligned in bf16
+        if ((p.lda * 2) % 16 || (p.ldb * 2) % 16 || (p.batch > 1 && ((p.stride_a * 2) % 16 || (p.stride_b * 2) % 16)))
+            return fail(TL_ERR_UNSUPPORTED, "bf16x3: lda/ldb (and batch strides) must be multiples of 8 elements");
+    }
+    return TL_SUCCESS;
+}
+
+tl_status enqueue(tl_handle* h, const Prepared& P, cudaStream_t s)
+{
+    const tl_gemm_problem& p = P.p;
+    if (p.m == 0 || p.n == 0) return TL_SUCCESS;
+    const float alpha = p.alpha * scale_of(p.scale_a) * scale_of(p.scale_b);
+    if (p.k == 0 || alpha == 0.0f) {
+        return aux_scale_c(p.dtype_d, p.out_rounding, P.D, p.ldd, p.stride_d, P.C, p.ldc, p.stride_c, p.m, p.n,
+                           p.batch, p.beta, s, &h->launches);
+    }
+    if (P.kernel == TL_KERNEL_SIMT) {
+        SimtLaunch L;
+        L.a_dtype = p.dtype_a; L.out_dtype = p.dtype_d; L.out_trunc = p.out_rounding;
+        L.trans_a = p.trans_a; L.trans_b = p.trans_b;
+        L.M = p.m; L.N = p.n; L.K = p.k; L.batch = p.batch;
+        L.A = P.A; L.B = P.B; L.C = P.C; L.D = P.D;
+        L.lda = p.lda; L.ldb = p.ldb; L.ldc = p.ldc; L.ldd = p.ldd;
+        L.sa = p.stride_a; L.sb = p.stride_b; L.sc = p.stride_c; L.sd = p.stride_d;
+        L.alpha = alpha; L.beta = p.beta;
+        return simt_gemm_launch(L, s, &h->launches);
+    }
+    TcLaunch L;
+    memset(&L, 0, sizeof(L));
+    L.in_dtype = tc_in_dtype(p);
+    L.out_dtype = p.dtype_d;
+    L.out_trunc = p.out_rounding;
+    L.x3 = (P.kernel == TL_KERNEL_BF16X3);
+    const void* A = P.A;
+    const void* B = P.B;
+    if (L.x3) {
+        const int64_t a_rows = p.trans_a ? p.k : p.m, a_cols = p.trans_a ? p.m : p.k;
+        const int64_t b_rows = p.trans_b ? p.n : p.k, b_cols = p.trans_b ? p.k : p.n;
+        tl_status st = aux_split_bf16x2(static_cast<const float*>(P.A), a_rows, a_cols, p.lda, p.batch, p.stride_a,
+                                        P.a_hi, P.a_lo, s, &h->launches);
+        if (st != TL_SUCCESS) return st;
+        st = aux_split_bf16x2(static_cast<const float*>(P.B), b_rows, b_cols, p.ldb, p.batch, p.stride_b, P.b_hi,
+                              P.b_lo, s, &h->launches);
+        if (st != TL_SUCCESS) return st;
+        A = P.a_hi;
+        B = P.b_hi;
+        L.opM_lo = {P.a_lo, p.m, p.lda, p.stride_a, m_mn_major(p) ? 1 : 0};
+        L.opN_lo = {P.b_lo, p.n, p.ldb, p.stride_b, n_mn_major(p) ? 1 : 0};
+    }
+    L.opM = {A, p.m, p.lda, p.stride_a, m_mn_major(p) ? 1 : 0};
+    L.opN = {B, p.n, p.ldb, p.stride_b, n_mn_major(p) ? 1 : 0};
+    L.M = p.m; L.N = p.n; L.K = p.k; L.batch = p.batch;
+    L.D = P.D; L.C = (p.beta != 0.0f) ? P.C : nullptr;
+    L.ldd = p.ldd; L.ldc = p.ldc; L.stride_d = p.stride_d; L.stride_c = p.stride_c;
+    L.alpha = alpha; L.beta = p.beta;
+    L.bm = P.s.macro_tile0;
+    L.stages = P.s.stages;
+    L.split_k = P.s.split_k;
+    L.raster = P.s.raster;
+    L.ctas = P.s.ctas;
+    L.err = h->d_err;
+    L.timeout_ns = h->timeout_ns;
+    L.workspace = P.ws_partials;
+    L.counters = h->counters;
+    L.sm_count = h->sm_count;
+    return tc_gemm_launch(L, s, &h->launches);
+}
+
+// ---- tuner ------------------------------------------------------------------------------------------
+std::vector<tl_gemm_solution> tc_candidates(const tl_handle* h, const tl_gemm_problem& p, int kernel)
+{
+    std::vector<std::pair<double, tl_gemm_solution>> ranked;
+    const int in = (kernel == TL_KERNEL_BF16X3) ? TL_DTYPE_BF16 : p.dtype_a;
+    const int W = row_elems(in);
+    const int64_t num_kb = std::max<int64_t>(1, (p.k + W - 1) / W);
+    const int64_t tiles_n = (p.n + kTcTileN - 1) / kTcTileN;
+    for (int bm : {64, 128, 192, 256}) {
+        for (int split : {1, 2, 3, 4, 6, 8, 12, 16}) {
+            if (split > num_kb) continue;
+            for (int raster : {0, 4, 8, 16}) {
+                tl_gemm_solution s;
+                memset(&s, 0, sizeof(s));
+                s.kernel = kernel;
+                s.macro_tile0 = bm;
+                s.macro_tile1 = kTcTileN;
+                s.depth_u = W;
+                s.stages = max_stages(bm, h->smem_optin);
+                s.split_k = split;
+                s.raster = raster;
+                if (raster && raster >= tiles_n) continue;
+                if (check_tc_solution(h, p, s) != TL_SUCCESS) continue;
+                // cost model: tensor work per tile grows with bm (efficiency of the 128 x bm MMA),
+                // waves quantise, split-k adds a partial round trip
+                const int64_t tiles = tiles_n * ((p.m + bm - 1) / bm) * p.batch;
+                const int64_t work = tiles * split;
+                const double waves = std::ceil(static_cast<double>(work) / h->sm_count);
+                const double per_unit = (static_cast<double>(bm) / 256.0 + 0.15) * (static_cast<double>(num_kb) / split + 4.0);
+                double cost = waves * per_unit;
+                if (split > 1) cost *= 1.0 + 0.02 * split;
+                if (raster == 0 && tiles_n > 8) cost *= 1.02;
+                ranked.push_back({cost, s});
+            }
+        }
+    }
+    std::stable_sort(ranked.begin(), ranked.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    std::vector<tl_gemm_solution> out;
+    for (auto& r : ranked) out.push_back(r.second);
+    return out;
+}
+
+tl_status save_cache(const char* path, const std::string& key, const tl_gemm_solution& s, float ms)
+{
+    // line-oriented JSON object: "key": [kernel, mt0, mt1, du, stages, wt0, wt1, split, raster, ctas, ms]
+    std::map<std::string, std::string> lines;
+    {
+        std::ifstream in(path);
+        std::string line;
+        while (std::getline(in, line)) {
+            size_t q0 = line.find('"');
+            size_t q1 = line.find("\":", q0 + 1);
+            if (q0 == std::string::npos || q1 == std::string::npos) continue;
+            std::string k = line.substr(q0 + 1, q1 - q0 - 1);
+            std::string v = line.substr(q1 + 2);
+            while (!v.empty() && (v.back() == ',' || v.back() == ' ' || v.back() == '\r')) v.pop_back();
+            lines[k] = v;
+        }
+    }
+    char buf[256];
+    snprintf(buf, sizeof(buf), " [%d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %.6f]", s.kernel, s.macro_tile0,
+             s.macro_tile1, s.depth_u, s.stages, s.wave_tile0, s.wave_tile1, s.split_k, s.raster, s.ctas, ms);
+    lines[key] = buf;
+    std::ofstream out(path, std::ios::trunc);
+    if (!out) return fail(TL_ERR_INVALID_ARG, std::string("cannot write ") + path);
+    out << "{\n";
+    size_t i = 0;
+    for (auto& kv : lines) {
+        out << "\"" << kv.first << "\":" << kv.second << (++i < lines.size() ? ",\n" : "\n");
+    }
+    out << "}\n";
+    return TL_SUCCESS;
+}
+
+}  // namespace
+}  // namespace tl
+
+using namespace tl;
+
+// =====================================================================================================
+// C ABI
+// =====================================================================================================
+extern "C" {
+
+TL_API const char* tl_last_error_string(void) { return g_last_error.c_str(); }
+
+TL_API const char* tl_status_string(tl_status st)
+{
+    switch (st) {
+    case TL_SUCCESS: return "TL_SUCCESS";
+    case TL_WARN: return "TL_WARN";
+    case TL_ERR: return "TL_ERR";
+    case TL_FATAL: return "TL_FATAL";
+    case TL_ERR_INVALID_ARG: return "TL_ERR_INVALID_ARG";
+    case TL_ERR_UNSUPPORTED: return "TL_ERR_UNSUPPORTED";
+    case TL_ERR_TIMEOUT: return "TL_ERR_TIMEOUT";
+    case TL_ERR_CUDA: return "TL_ERR_CUDA";
+    case TL_ERR_ALLOC: return "TL_ERR_ALLOC";
+    default: return "TL_UNKNOWN";
+    }
+}
+
+TL_API int tl_version(void) { return 10000; }
+
+TL_API tl_status tl_init(tl_handle** handle)
+{
+    if (!handle) return fail(TL_ERR_INVALID_ARG, "handle out-pointer is NULL");
+    *handle = nullptr;
+    tl_handle* h = new (std::nothrow) tl_handle();
+    if (!h) return fail(TL_ERR_ALLOC, "handle allocation failed");
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaGetDevice"); }
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, h->device);
+    if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaGetDeviceProperties"); }
+    h->sm_count = prop.multiProcessorCount;
+    h->cc_major = prop.major;
+    h->cc_minor = prop.minor;
+    h->smem_optin = prop.sharedMemPerBlockOptin;
+    snprintf(h->name, sizeof(h->name), "%s", prop.name);
+    if (const char* t = getenv("TL_WAIT_TIMEOUT_MS")) {
+        long v = strtol(t, nullptr, 10);
+        if (v > 0) h->timeout_ns = static_cast<uint64_t>(v) * 1000000ull;
+    }
+    if ((e = cudaMalloc(&h->d_err, 256)) != cudaSuccess) { delete h; return cuda_fail(e, "cudaMalloc(err)"); }
+    h->d_norms = reinterpret_cast<double*>(reinterpret_cast<char*>(h->d_err) + 64);
+    h->d_amax = reinterpret_cast<float*>(reinterpret_cast<char*>(h->d_err) + 128);
+    if ((e = cudaMemset(h->d_err, 0, 256)) != cudaSuccess) { cudaFree(h->d_err); delete h; return cuda_fail(e, "cudaMemset"); }
+    *handle = h;
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_destroy(tl_handle* h)
+{
+    if (!h) return TL_SUCCESS;
+    cudaDeviceSynchronize();
+    if (h->ws) cudaFree(h->ws);
+    if (h->counters) cudaFree(h->counters);
+    if (h->d_err) cudaFree(h->d_err);
+    delete h;
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_device_info(tl_handle* h, int* sm_count, int* cc_major, int* cc_minor, size_t* smem)
+{
+    if (!h) return fail(TL_ERR_INVALID_ARG, "handle is NULL");
+    if (sm_count) *sm_count = h->sm_count;
+    if (cc_major) *cc_major = h->cc_major;
+    if (cc_minor) *cc_minor = h->cc_minor;
+    if (smem) *smem = h->smem_optin;
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_problem_init(tl_gemm_problem* p, tl_dtype ab, tl_dtype cd, tl_op ta, tl_op tb, int64_t m,
+                                 int64_t n, int64_t k)
+{
+    if (!p) return fail(TL_ERR_INVALID_ARG, "problem is NULL");
+    memset(p, 0, sizeof(*p));
+    p->dtype_a = p->dtype_b = ab;
+    p->dtype_c = p->dtype_d = cd;
+    p->trans_a = ta;
+    p->trans_b = tb;
+    p->m = m; p->n = n; p->k = k;
+    p->batch = 1;
+    p->lda = std::max<int64_t>(1, ta == TL_OP_N ? m : k);
+    p->ldb = std::max<int64_t>(1, tb == TL_OP_N ? k : n);
+    p->ldc = p->ldd = std::max<int64_t>(1, m);
+    p->stride_a = p->lda * (ta == TL_OP_N ? k : m);
+    p->stride_b = p->ldb * (tb == TL_OP_N ? n : k);
+    p->stride_c = p->stride_d = p->ldd * n;
+    p->alpha = 1.0f;
+    p->beta = 0.0f;
+    p->scale_a = p->scale_b = 1.0f;
+    p->kernel = TL_KERNEL_AUTO;
+    p->out_rounding = TL_ROUND_RNE;
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_default_solution(tl_handle* h, const tl_gemm_problem* p, tl_gemm_solution* s)
+{
+    if (!h || !s) return fail(TL_ERR_INVALID_ARG, "NULL argument");
+    tl_status st = validate(p);
+    if (st != TL_SUCCESS) return st;
+    const int kernel = resolve_kernel(*p);
+    if (kernel == TL_KERNEL_SIMT) simt_solution(s);
+    else tc_heuristic(h, *p, kernel, s);
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_check_solution(tl_handle* h, const tl_gemm_problem* p, const tl_gemm_solution* s)
+{
+    if (!h || !s) return fail(TL_ERR_INVALID_ARG, "NULL argument");
+    tl_status st = validate(p);
+    if (st != TL_SUCCESS) return st;
+    if (s->kernel == TL_KERNEL_SIMT) {
+        if (s->macro_tile0 != 128 || s->macro_tile1 != 128 || (s->depth_u && s->depth_u != 8) || s->split_k > 1)
+            return fail(TL_ERR_UNSUPPORTED, "SIMT kernel supports macro tile 128x128, depth_u 8, split_k 1");
+        return TL_SUCCESS;
+    }
+    if (s->kernel != TL_KERNEL_TCGEN05 && s->kernel != TL_KERNEL_BF16X3)
+        return fail(TL_ERR_INVALID_ARG, "solution kernel must be resolved (SIMT, TCGEN05 or BF16X3)");
+    if (s->kernel == TL_KERNEL_BF16X3 && p->dtype_a != TL_DTYPE_FP32)
+        return fail(TL_ERR_UNSUPPORTED, "bf16x3 needs fp32 inputs");
+    if (s->kernel == TL_KERNEL_TCGEN05 && p->dtype_a == TL_DTYPE_FP32)
+        return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel needs fp16/bf16/fp8 inputs");
+    return check_tc_solution(h, *p, *s);
+}
+
+TL_API tl_status tl_gemm(tl_handle* h, const tl_gemm_problem* p, const tl_gemm_solution* s, void* D, const void* C,
+                         const void* A, const void* B, void* stream)
+{
+    if (!h) return fail(TL_ERR_INVALID_ARG, "handle is NULL");
+    Prepared P;
+    tl_status st = prepare(h, p, s, D, C, A, B, &P);
+    if (st != TL_SUCCESS) return st;
+    return enqueue(h, P, S(stream));
+}
+
+TL_API tl_status tl_tune(tl_handle* h, const tl_gemm_problem* p, void* D, const void* C, const void* A,
+                         const void* B, int max_candidates, int reps, const char* cache_path, tl_gemm_solution* best,
+                         float* best_ms)
+{
+    if (!h || !best) return fail(TL_ERR_INVALID_ARG, "NULL argument");
+    tl_status st = validate(p);
+    if (st != TL_SUCCESS) return st;
+    const int kernel = resolve_kernel(*p);
+    std::vector<tl_gemm_solution> cands;
+    if (kernel == TL_KERNEL_SIMT) {
+        tl_gemm_solution s;
+        simt_solution(&s);
+        cands.push_back(s);
+    } else {
+        cands = tc_candidates(h, *p, kernel);
+    }
+    if (cands.empty()) return fail(TL_ERR_UNSUPPORTED, "no legal candidate solution");
+    if (max_candidates <= 0) max_candidates = 16;
+    if (reps <= 0) reps = 10;
+    if (static_cast<int>(cands.size()) > max_candidates) cands.resize(max_candidates);
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return fail(TL_ERR_CUDA, "stream create");
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best_t = 1e30f;
+    tl_gemm_solution best_s = cands[0];
+    bool any = false;
+    for (const auto& c : cands) {
+        Prepared P;
+        if (prepare(h, p, &c, D, C, A, B, &P) != TL_SUCCESS) continue;
+        if (enqueue(h, P, s) != TL_SUCCESS) continue;          // warm-up
+        if (cudaStreamSynchronize(s) != cudaSuccess) { cudaGetLastError(); continue; }
+        cudaEventRecord(e0, s);
+        bool ok = true;
+        for (int r = 0; r < reps && ok; ++r) ok = enqueue(h, P, s) == TL_SUCCESS;
+        cudaEventRecord(e1, s);
+        if (!ok || cudaEventSynchronize(e1) != cudaSuccess) continue;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= reps;
+        any = true;
+        if (ms < best_t) { best_t = ms; best_s = c; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(s);
+    if (!any) return fail(TL_ERR_UNSUPPORTED, "every candidate failed: " + g_last_error);
+    *best = best_s;
+    if (best_ms) *best_ms = best_t;
+    const std::string key = problem_key(h, *p);
+    {
+        std::lock_guard<std::mutex> g(h->mu);
+        h->tuned[key] = best_s;
+    }
+    if (cache_path) return save_cache(cache_path, key, best_s, best_t);
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_load_solutions(tl_handle* h, const char* path, int* loaded)
+{
+    if (!h || !path) return fail(TL_ERR_INVALID_ARG, "NULL argument");
+    std::ifstream in(path);
+    if (!in) return fail(TL_ERR_INVALID_ARG, std::string("cannot read ") + path);
+    std::string line;
+    int n = 0;
+    const std::string prefix = std::string(h->name) + "|sm" + std::to_string(h->cc_major) + std::to_string(h->cc_minor) + "|";
+    while (std::getline(in, line)) {
+        size_t q0 = line.find('"');
+        size_t q1 = line.find("\":", q0 + 1);
+        size_t b0 = line.find('[', q1 == std::string::npos ? 0 : q1);
+        if (q0 == std::string::npos || q1 == std::string::npos || b0 == std::string::npos) continue;
+        std::string key = line.substr(q0 + 1, q1 - q0 - 1);
+        if (key.compare(0, prefix.size(), prefix) != 0) continue;   // other device
+        tl_gemm_solution s;
+        memset(&s, 0, sizeof(s));
+        float ms = 0;
+        if (sscanf(line.c_str() + b0, "[%d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %f", &s.kernel, &s.macro_tile0,
+                   &s.macro_tile1, &s.depth_u, &s.stages, &s.wave_tile0, &s.wave_tile1, &s.split_k, &s.raster, &s.ctas,
+                   &ms) == 11) {
+            std::lock_guard<std::mutex> g(h->mu);
+            h->tuned[key] = s;
+            ++n;
+        }
+    }
+    if (loaded) *loaded = n;
+    return TL_SUCCESS;
+}
+
+// ---- grouped ---------------------------------------------------------------------------------------
+TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* probs, int count, void* const* D,
+                                        const void* const* C, const void* const* A, const void* const* B,
+                                        const tl_gemm_solution* sol, tl_grouped_plan** plan)
+{
+    if (!h || !probs || !plan || count < 1 || !D || !A || !B) return fail(TL_ERR_INVALID_ARG, "NULL argument or count < 1");
+    *plan = nullptr;
+    const tl_gemm_problem& p0 = probs[0];
+    tl_status st;
+    for (int i = 0; i < count; ++i) {
+        const tl_gemm_problem& p = probs[i];
+        if ((st = validate(&p)) != TL_SUCCESS) return fail(st, "problem " + std::to_string(i) + ": " + g_last_error);
+        if (p.dtype_a != p0.dtype_a || p.dtype_d != p0.dtype_d || p.trans_a != p0.trans_a || p.trans_b != p0.trans_b ||
+            p.out_rounding != p0.out_rounding)
+            return fail(TL_ERR_UNSUPPORTED, "grouped problems must share dtypes, trans flags and rounding");
+        if (p.batch != 1) return fail(TL_ERR_UNSUPPORTED, "grouped problems must have batch == 1");
+        if (p.k == 0) return fail(TL_ERR_UNSUPPORTED, "grouped problems need k > 0");
+        if (p.beta != 0.0f && (!C || !C[i])) return fail(TL_ERR_INVALID_ARG, "C missing with beta != 0");
+        std::string why;
+        tl_gemm_problem q = p;
+        q.kernel = TL_KERNEL_TCGEN05;
+        if (!tma_ok(q, A[i], B[i], &why)) return fail(TL_ERR_UNSUPPORTED, "problem " + std::to_string(i) + ": " + why);
+    }
+    if (p0.dtype_a != TL_DTYPE_FP16 && p0.dtype_a != TL_DTYPE_BF16 && p0.dtype_a != TL_DTYPE_FP8_E4M3)
+        return fail(TL_ERR_UNSUPPORTED, "grouped GEMM takes fp16/bf16/fp8 operands");
+    tl_gemm_solution s;
+    if (sol) {
+        s = *sol;
+    } else {
+        // heuristic for a group: the tile that suits the median problem
+        std::vector<int64_t> ms;
+        for (int i = 0; i < count; ++i) ms.push_back(probs[i].m);
+        std::nth_element(ms.begin(), ms.begin() + count / 2, ms.end());
+        tl_gemm_problem med = p0;
+        med.m = ms[count / 2];
+        med.kernel = TL_KERNEL_TCGEN05;
+        tc_heuristic(h, med, TL_KERNEL_TCGEN05, &s);
+        s.macro_tile0 = 256;
+        if (m_mn_major(p0) && p0.dtype_a == TL_DTYPE_FP8_E4M3) s.macro_tile0 = 256;
+        s.stages = max_stages(s.macro_tile0, h->smem_optin);
+        s.split_k = 1;
+        s.raster = 0;
+    }
+    s.kernel = TL_KERNEL_TCGEN05;
+    if (s.split_k != 1) return fail(TL_ERR_UNSUPPORTED, "grouped GEMM does not split k");
+    for (int i = 0; i < count; ++i)
+        if ((st = check_tc_solution(h, probs[i], s)) != TL_SUCCESS) return st;
+
+    std::vector<TcGroupEntry> host(count);
+    std::vector<int64_t> prefix(count + 1, 0);
+    double flops = 0;
+    for (int i = 0; i < count; ++i) {
+        const tl_gemm_problem& p = probs[i];
+        TcGroupEntry& e = host[i];
+        memset(&e, 0, sizeof(e));
+        TcOperand opN{B[i], p.n, p.ldb, p.stride_b, n_mn_major(p) ? 1 : 0};
+        TcOperand opM{A[i], p.m, p.lda, p.stride_a, m_mn_major(p) ? 1 : 0};
+        if (p.m > 0 && p.n > 0) {
+            if ((st = tc_encode_operand(&e.tmN, p.dtype_a, opN, p.k, 1, kTcTileN)) != TL_SUCCESS) return st;
+            if ((st = tc_encode_operand(&e.tmM, p.dtype_a, opM, p.k, 1, s.macro_tile0)) != TL_SUCCESS) return st;
+        }
+        e.D = D[i];
+        e.C = (p.beta != 0.0f && C) ? C[i] : nullptr;
+        e.ldd = p.ldd;
+        e.ldc = p.ldc;
+        e.M = static_cast<int32_t>(p.m);
+        e.N = static_cast<int32_t>(p.n);
+        e.K = static_cast<int32_t>(p.k);
+        e.tiles_m = static_cast<int32_t>((p.m + s.macro_tile0 - 1) / s.macro_tile0);
+        e.tiles_n = static_cast<int32_t>((p.n + kTcTileN - 1) / kTcTileN);
+        e.alpha = p.alpha * scale_of(p.scale_a) * scale_of(p.scale_b);
+        e.beta = p.beta;
+        prefix[i + 1] = prefix[i] + static_cast<int64_t>(e.tiles_m) * e.tiles_n;
+        flops += 2.0 * static_cast<double>(p.m) * p.n * p.k;
+    }
+    tl_grouped_plan* pl = new (std::nothrow) tl_grouped_plan();
+    if (!pl) return fail(TL_ERR_ALLOC, "plan allocation failed");
+    pl->h = h;
+    cudaError_t e;
+    if ((e = cudaMalloc(&pl->d_entries, sizeof(TcGroupEntry) * count)) != cudaSuccess ||
+        (e = cudaMalloc(&pl->d_prefix, sizeof(int64_t) * (count + 1))) != cudaSuccess) {
+        tl_grouped_plan_destroy(pl);
+        return cuda_fail(e, "cudaMalloc(plan)");
+    }
+    if ((e = cudaMemcpy(pl->d_entries, host.data(), sizeof(TcGroupEntry) * count, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(pl->d_prefix, prefix.data(), sizeof(int64_t) * (count + 1), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        tl_grouped_plan_destroy(pl);
+        return cuda_fail(e, "cudaMemcpy(plan)");
+    }
+    TcGroupLaunch& G = pl->launch;
+    G.in_dtype = p0.dtype_a;
+    G.out_dtype = p0.dtype_d;
+    G.out_trunc = p0.out_rounding;
+    G.n_mn_major = n_mn_major(p0) ? 1 : 0;
+    G.m_mn_major = m_mn_major(p0) ? 1 : 0;
+    G.d_entries = pl->d_entries;
+    G.d_tile_prefix = pl->d_prefix;
+    G.count = count;
+    G.total_tiles = prefix[count];
+    G.bm = s.macro_tile0;
+    G.stages = s.stages;
+    G.ctas = s.ctas;
+    G.err = h->d_err;
+    G.timeout_ns = h->timeout_ns;
+    G.sm_count = h->sm_count;
+    pl->sol = s;
+    pl->flops = flops;
+    *plan = pl;
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_grouped_plan_launch(tl_grouped_plan* pl, void* stream)
+{
+    if (!pl) return fail(TL_ERR_INVALID_ARG, "plan is NULL");
+    if (pl->launch.total_tiles == 0) return TL_SUCCESS;
+    return tc_grouped_launch(pl->launch, S(stream), &pl->h->launches);
+}
+
+TL_API tl_status tl_grouped_plan_destroy(tl_grouped_plan* pl)
+{
+    if (!pl) return TL_SUCCESS;
+    if (pl->d_entries || pl->d_prefix) cudaDeviceSynchronize();
+    if (pl->d_entries) cudaFree(pl->d_entries);
+    if (pl->d_prefix) cudaFree(pl->d_prefix);
+    delete pl;
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_grouped_plan_info(const tl_grouped_plan* pl, double* flops, int64_t* tiles, tl_gemm_solution* s)
+{
+    if (!pl) return fail(TL_ERR_INVALID_ARG, "plan is NULL");
+    if (flops) *flops = pl->flops;
+    if (tiles) *tiles = pl->launch.total_tiles;
+    if (s) *s = pl->sol;
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_gemm_grouped(tl_handle* h, const tl_gemm_problem* probs, int count, void* const* D,
+                                 const void* const* C, const void* const* A, const void* const* B, void* stream)
+{
+    tl_grouped_plan* pl = nullptr;
+    tl_status st = tl_grouped_plan_create(h, probs, count, D, C, A, B, nullptr, &pl);
+    if (st != TL_SUCCESS) return st;
+    st = tl_grouped_plan_launch(pl, stream);
+    if (st == TL_SUCCESS) {
+        cudaError_t e = cudaStreamSynchronize(S(stream));
+        if (e != cudaSuccess) st = cuda_fail(e, "cudaStreamSynchronize(grouped)");
+    }
+    tl_grouped_plan_destroy(pl);
+    return st;
+}
+
+TL_API tl_status tl_tune_grouped(tl_handle* h, const tl_gemm_problem* probs, int count, void* const* D,
+                                 const void* const* C, const void* const* A, const void* const* B, int reps,
+                                 tl_gemm_solution* best, float* best_ms)
+{
+    if (!h || !best || count < 1) return fail(TL_ERR_INVALID_ARG, "NULL argument");
+    if (reps <= 0) reps = 5;
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return fail(TL_ERR_CUDA, "stream create");
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best_t = 1e30f;
+    bool any = false;
+    for (int bm : {64, 128, 192, 256}) {
+        for (int stages : {3, 4, 6, 8}) {
+            tl_gemm_solution c;
+            memset(&c, 0, sizeof(c));
+            c.kernel = TL_KERNEL_TCGEN05;
+            c.macro_tile0 = bm;
+            c.macro_tile1 = kTcTileN;
+            c.stages = std::min(stages, max_stages(bm, h->smem_optin));
+            c.split_k = 1;
+            if (stages > c.stages) continue;
+            tl_grouped_plan* pl = nullptr;
+            if (tl_grouped_plan_create(h, probs, count, D, C, A, B, &c, &pl) != TL_SUCCESS) continue;
+            bool ok = tl_grouped_plan_launch(pl, s) == TL_SUCCESS && cudaStreamSynchronize(s) == cudaSuccess;
+            if (ok) {
+                cudaEventRecord(e0, s);
+                for (int r = 0; r < reps && ok; ++r) ok = tl_grouped_plan_launch(pl, s) == TL_SUCCESS;
+                cudaEventRecord(e1, s);
+                ok = ok && cudaEventSynchronize(e1) == cudaSuccess;
+            }
+            if (ok) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                ms /= reps;
+                any = true;
+                if (ms < best_t) { best_t = ms; *best = pl->sol; }
+            }
+            tl_grouped_plan_destroy(pl);
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(s);
+    if (!any) return fail(TL_ERR_UNSUPPORTED, "every grouped candidate failed: " + g_last_error);
+    if (best_ms) *best_ms = best_t;
+    return TL_SUCCESS;
+}
+
+// ---- graphs ----------------------------------------------------------------------------------------
+static tl_status end_capture(cudaStream_t s, tl_status inner, tl_graph** out)
+{
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (inner != TL_SUCCESS) {
+        if (g) cudaGraphDestroy(g);
+        return inner;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    tl_graph* gr = new (std::nothrow) tl_graph();
+    if (!gr) { cudaGraphDestroy(g); return fail(TL_ERR_ALLOC, "graph allocation failed"); }
+    gr->graph = g;
+    e = cudaGraphInstantiate(&gr->exec, g, 0);
+    if (e != cudaSuccess) { cudaGraphDestroy(g); delete gr; return cuda_fail(e, "cudaGraphInstantiate"); }
+    *out = gr;
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_graph_capture_grouped(tl_grouped_plan* pl, void* stream, tl_graph** out)
+{
+    if (!pl || !out || !stream) return fail(TL_ERR_INVALID_ARG, "NULL argument (capture needs a non-default stream)");
+    cudaStream_t s = S(stream);
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCapture");
+    tl_status st = tl_grouped_plan_launch(pl, stream);
+    return end_capture(s, st, out);
+}
+
+TL_API tl_status tl_graph_capture_gemm(tl_handle* h, const tl_gemm_problem* p, const tl_gemm_solution* sol, void* D,
+                                       const void* C, const void* A, const void* B, void* stream, tl_graph** out)
+{
+    if (!h || !out || !stream) return fail(TL_ERR_INVALID_ARG, "NULL argument (capture needs a non-default stream)");
+    Prepared P;
+    tl_status st = prepare(h, p, sol, D, C, A, B, &P);   // allocations happen before capture
+    if (st != TL_SUCCESS) return st;
+    cudaStream_t s = S(stream);
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCapture");
+    st = enqueue(h, P, s);
+    return end_capture(s, st, out);
+}
+
+TL_API tl_status tl_graph_launch(tl_graph* g, void* stream)
+{
+    if (!g) return fail(TL_ERR_INVALID_ARG, "graph is NULL");
+    TL_CUDA_TRY(cudaGraphLaunch(g->exec, S(stream)));
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_graph_destroy(tl_graph* g)
+{
+    if (!g) return TL_SUCCESS;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
+    return TL_SUCCESS;
+}
+
+// ---- fp8 / split -------------------------------------------------------------------------------------
+TL_API tl_status tl_quantize_fp8(tl_handle* h, tl_dtype src_dtype, const void* src, int64_t n, void* dst,
+                                 float* scale_out, float* amax_out, void* stream)
+{
+    if (!h || (!src && n) || (!dst && n) || n < 0) return fail(TL_ERR_INVALID_ARG, "bad argument");
+    if (src_dtype != TL_DTYPE_FP32 && src_dtype != TL_DTYPE_FP16 && src_dtype != TL_DTYPE_BF16)
+        return fail(TL_ERR_UNSUPPORTED, "quantize: source must be fp32, fp16 or bf16");
+    float* amax = amax_out ? amax_out : h->d_amax;
+    tl_status st = aux_amax(src_dtype, src, n, amax, S(stream), &h->launches);
+    if (st != TL_SUCCESS) return st;
+    return aux_quant_e4m3(src_dtype, src, n, amax, static_cast<uint8_t*>(dst), scale_out, S(stream), &h->launches);
+}
+
+TL_API tl_status tl_split_bf16x2(tl_handle* h, const float* src, int64_t n, void* hi, void* lo, void* stream)
+{
+    if (!h || n < 0 || (n && (!src || !hi || !lo))) return fail(TL_ERR_INVALID_ARG, "bad argument");
+    return aux_split_bf16x2(src, n, 1, n, 1, n, static_cast<uint16_t*>(hi), static_cast<uint16_t*>(lo), S(stream),
+                            &h->launches);
+}
+
+// ---- verification ------------------------------------------------------------------------------------
+TL_API tl_status tl_error_norms(tl_handle* h, tl_dtype dtype_d, const void* D, int64_t ldd, const double* R,
+                                const double* W, int64_t ldr, int64_t m, int64_t n, double out[3], void* stream)
+{
+    if (!h || !out || m < 0 || n < 0 || ldd < m || ldr < m) return fail(TL_ERR_INVALID_ARG, "bad argument");
+    if (dtype_bytes(dtype_d) == 0) return fail(TL_ERR_INVALID_ARG, "bad dtype");
+    tl_status st = aux_error_norms(dtype_d, D, ldd, R, W, ldr, m, n, h->d_norms, S(stream), &h->launches);
+    if (st != TL_SUCCESS) return st;
+    TL_CUDA_TRY(cudaMemcpyAsync(out, h->d_norms, 3 * sizeof(double), cudaMemcpyDeviceToHost, S(stream)));
+    TL_CUDA_TRY(cudaStreamSynchronize(S(stream)));
+    return TL_SUCCESS;
+}
+
+// ---- buffers -------------------------------------------------------------------------------------
+TL_API tl_status tl_malloc(void** p, size_t bytes)
+{
+    if (!p) return fail(TL_ERR_INVALID_ARG, "NULL out-pointer");
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 1);
+    if (e != cudaSuccess) { *p = nullptr; return fail(TL_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e)); }
+    return TL_SUCCESS;
+}
+TL_API tl_status tl_free(void* p) { TL_CUDA_TRY(cudaFree(p)); return TL_SUCCESS; }
+TL_API tl_status tl_host_malloc(void** p, size_t bytes)
+{
+    if (!p) return fail(TL_ERR_INVALID_ARG, "NULL out-pointer");
+    cudaError_t e = cudaMallocHost(p, bytes ? bytes : 1);
+    if (e != cudaSuccess) { *p = nullptr; return fail(TL_ERR_ALLOC, std::string("cudaMallocHost: ") + cudaGetErrorString(e)); }
+    return TL_SUCCESS;
+}
+TL_API tl_status tl_host_free(void* p) { TL_CUDA_TRY(cudaFreeHost(p)); return TL_SUCCESS; }
+TL_API tl_status tl_memcpy_h2d(void* d, const void* s, size_t b, void* st)
+{ TL_CUDA_TRY(cudaMemcpyAsync(d, s, b, cudaMemcpyHostToDevice, S(st))); return TL_SUCCESS; }
+TL_API tl_status tl_memcpy_d2h(void* d, const void* s, size_t b, void* st)
+{ TL_CUDA_TRY(cudaMemcpyAsync(d, s, b, cudaMemcpyDeviceToHost, S(st))); return TL_SUCCESS; }
+TL_API tl_status tl_memcpy_d2d(void* d, const void* s, size_t b, void* st)
+{ TL_CUDA_TRY(cudaMemcpyAsync(d, s, b, cudaMemcpyDeviceToDevice, S(st))); return TL_SUCCESS; }
+TL_API tl_status tl_memset(void* d, int v, size_t b, void* st)
+{ TL_CUDA_TRY(cudaMemsetAsync(d, v, b, S(st))); return TL_SUCCESS; }
+TL_API tl_status tl_stream_create(void** s)
+{
+    if (!s) return fail(TL_ERR_INVALID_ARG, "NULL out-pointer");
+    cudaStream_t st;
+    TL_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    *s = st;
+    return TL_SUCCESS;
+}
+TL_API tl_status tl_stream_destroy(void* s) { TL_CUDA_TRY(cudaStreamDestroy(S(s))); return TL_SUCCESS; }
+TL_API tl_status tl_stream_synchronize(void* s) { TL_CUDA_TRY(cudaStreamSynchronize(S(s))); return TL_SUCCESS; }
+
+TL_API tl_status tl_fill_pattern(tl_dtype dtype, void* dst, int64_t count, float code, void* stream)
+{
+    if (dtype_bytes(dtype) == 0 || count < 0 || (count && !dst)) return fail(TL_ERR_INVALID_ARG, "bad argument");
+    if (code == 2.2f || code == -2.2f)
+        return fail(TL_ERR_UNSUPPORTED, "patterns 2.2/-2.2 depend on the buffer shape; fill them on the host");
+    return aux_fill_pattern(dtype, dst, count, code, S(stream), nullptr);
+}
+
+// Host converters (IEEE round-to-nearest-even unless TRUNCATE is asked for bf16).
+static uint16_t host_f32_to_f16(float f)
+{
+    uint32_t x;
+    memcpy(&x, &f, 4);
+    const uint32_t sign = (x >> 16) & 0x8000u;
+    const uint32_t e = (x >> 23) & 0xffu;
+    const uint32_t man = x & 0x7fffffu;
+    if (e == 0xffu) return static_cast<uint16_t>(sign | 0x7c00u | (man ? 0x200u : 0u));
+    const int32_t he = static_cast<int32_t>(e) - 112;
+    if (he >= 31) return static_cast<uint16_t>(sign | 0x7c00u);
+    uint32_t sig = (e == 0) ? man : (man | 0x800000u);
+    int shift;
+    uint32_t base;
+    if (he >= 1) { shift = 13; base = static_cast<uint32_t>(he) << 10; sig &= 0x7fffffu; }
+    else { shift = 14 - he; base = 0; if (shift > 31) return static_cast<uint16_t>(sign); }
+    const uint32_t q = sig >> shift, rem = sig & ((1u << shift) - 1u), half = 1u << (shift - 1);
+    uint32_t r = base + q;
+    if (rem > half || (rem == half && (q & 1u))) ++r;
+    if (r >= 0x7c00u) r = 0x7c00u;
+    return static_cast<uint16_t>(sign | r);
+}
+static uint16_t host_f32_to_bf16(float f, int trunc)
+{
+    uint32_t x;
+    memcpy(&x, &f, 4);
+    if (trunc) return static_cast<uint16_t>(x >> 16);
+    if ((x & 0x7f800000u) == 0x7f800000u && (x & 0x7fffffu)) return static_cast<uint16_t>((x >> 16) | 0x40u);
+    x += 0x7fffu + ((x >> 16) & 1u);
+    return static_cast<uint16_t>(x >> 16);
+}
+
+TL_API tl_status tl_convert_host(const float* src, int64_t n, tl_dtype dtype, tl_rounding rounding, void* dst)
+{
+    if (n < 0 || (n && (!src || !dst))) return fail(TL_ERR_INVALID_ARG, "bad argument");
+    switch (dtype) {
+    case TL_DTYPE_FP32: memcpy(dst, src, static_cast<size_t>(n) * 4); break;
+    case TL_DTYPE_FP16:
+        for (int64_t i = 0; i < n; ++i) static_cast<uint16_t*>(dst)[i] = host_f32_to_f16(src[i]);
+        break;
+    case TL_DTYPE_BF16:
+        for (int64_t i = 0; i < n; ++i)
+            static_cast<uint16_t*>(dst)[i] = host_f32_to_bf16(src[i], rounding == TL_ROUND_TRUNCATE);
+        break;
+    default: return fail(TL_ERR_UNSUPPORTED, "host conversion to this dtype is not provided");
+    }
+    return TL_SUCCESS;
+}
+
+// ---- timers ------------------------------------------------------------------------------------------
+TL_API tl_status tl_timer_create(tl_timer** t)
+{
+    if (!t) return fail(TL_ERR_INVALID_ARG, "NULL out-pointer");
+    tl_timer* x = new (std::nothrow) tl_timer();
+    if (!x) return fail(TL_ERR_ALLOC, "timer allocation failed");
+    if (cudaEventCreate(&x->start) != cudaSuccess || cudaEventCreate(&x->stop) != cudaSuccess) {
+        delete x;
+        return fail(TL_ERR_CUDA, "cudaEventCreate");
+    }
+    *t = x;
+    return TL_SUCCESS;
+}
+TL_API tl_status tl_timer_start(tl_timer* t, void* s) { TL_CUDA_TRY(cudaEventRecord(t->start, S(s))); return TL_SUCCESS; }
+TL_API tl_status tl_timer_stop(tl_timer* t, void* s) { TL_CUDA_TRY(cudaEventRecord(t->stop, S(s))); return TL_SUCCESS; }
+TL_API tl_status tl_timer_elapsed_ms(tl_timer* t, float* ms)
+{
+    TL_CUDA_TRY(cudaEventSynchronize(t->stop));
+    TL_CUDA_TRY(cudaEventElapsedTime(ms, t->start, t->stop));
+    return TL_SUCCESS;
+}
+TL_API tl_status tl_timer_destroy(tl_timer* t)
+{
+    if (!t) return TL_SUCCESS;
+    cudaEventDestroy(t->start);
+    cudaEventDestroy(t->stop);
+    delete t;
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_launch_count(tl_handle* h, int64_t* n)
+{
+    if (!h || !n) return fail(TL_ERR_INVALID_ARG, "NULL argument");
+    *n = h->launches;
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_device_status(tl_handle* h, void* stream)
+{
+    if (!h) return fail(TL_ERR_INVALID_ARG, "handle is NULL");
+    cudaError_t e = cudaStreamSynchronize(S(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    int v = 0;
+    TL_CUDA_TRY(cudaMemcpy(&v, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (v) {
+        TL_CUDA_TRY(cudaMemset(h->d_err, 0, sizeof(int)));
+        char buf[128];
+        snprintf(buf, sizeof(buf), "device wait timed out (role mask 0x%x)", v);
+        return fail(TL_ERR_TIMEOUT, buf);
+    }
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_set_wait_timeout(tl_handle* h, uint32_t ms)
+{
+    if (!h || ms == 0) return fail(TL_ERR_INVALID_ARG, "bad argument");
+    h->timeout_ns = static_cast<uint64_t>(ms) * 1000000ull;
+    return TL_SUCCESS;
+}
+
+}  // extern "C"

@@ -1,0 +1,401 @@
+"""GPU parity: every kernel path through the C ABI against the oracle (the restated reference loop
+and the FP64 oracle) on the same seeded inputs.
+
+Tolerances (written here, per output type):
+  * 16-bit outputs: every element within ONE ulp of the output type of the oracle's fp32 result
+    rounded the same way (the accumulation order differs; its error is far below a 16-bit ulp).
+  * fp32 outputs: normwise error max|d - r| / max|r| against the oracle below 2e-6 * sqrt(k/512)
+    (both sides accumulate in fp32 in different orders).
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+import tensilelite_gb300 as tl
+from oracle import oracle as orc
+from tests import gpu_util as gu
+from tests.golden import gen_golden as gg
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module")
+def h():
+    import torch
+    torch.cuda.init()
+    os.environ.setdefault("TL_WAIT_TIMEOUT_MS", "2000")
+    hd = tl.Handle()
+    yield hd
+    hd.close()
+
+
+def fp32_tol(k):
+    return 2e-6 * math.sqrt(max(k, 512) / 512.0)
+
+
+def check_case(h, case, dt, kernel="auto", solution=None, rounding="rne"):
+    got = gu.run_case(h, case, kernel=kernel, dtype=dt, solution=solution, rounding=rounding)
+    ref = gu.oracle_ref(case)
+    m, n = case["m"], case["n"]
+    G = gu.mat(got, m, n, case["ldc"])
+    R = gu.mat(ref, m, n, m)
+    assert np.all(np.isfinite(G)), "non-finite output"
+    od = case["out_dtype"]
+    if od == "fp32":
+        err = orc.normwise_error(G, R)
+        assert err <= fp32_tol(case["k"]), f"normwise {err}"
+    else:
+        Rq = gu.quantize_out(R, od, rounding)
+        bad = gu.ulp_diff_count(G, Rq, od)
+        assert bad == 0, f"{bad} elements beyond 1 ulp; normwise {orc.normwise_error(G, R)}"
+    return G, R
+
+
+# ---------------------------------------------------------------------------- CUDA-core FP32 kernel
+def test_simt_fp32_480x512x512_nn(h):
+    """Plain FP32 GEMM, NN, 480x512x512, A/B uniform[-1,1) seed 0, alpha 1, beta 0."""
+    g = orc.rng(0)
+    M, N, K = 480, 512, 512
+    A = orc.uniform_pm1(g, M * K).astype(np.float32)
+    B = orc.uniform_pm1(g, K * N).astype(np.float32)
+    case = dict(trans_a=False, trans_b=False, m=M, n=N, k=K, lda=M, ldb=K, ldc=M, alpha=1.0, beta=0.0, A_bits=A,
+                B_bits=B, C_bits=np.zeros(M * N, np.float32), A=A, B=B, C=np.zeros(M * N, np.float32),
+                out_dtype="fp32")
+    G, R = check_case(h, case, "fp32", kernel="simt")
+    D64 = gu.mat(gu.oracle_f64(case), M, N, M)
+    assert orc.normwise_error(G, D64) < 1e-6
+
+
+@pytest.mark.parametrize("lay", gg.LAYOUTS)
+def test_simt_fp32_layouts_edges(h, lay):
+    case = gg.make_case("fp32", lay, 21 + gg.LAYOUTS.index(lay), 131, 67, 45)
+    check_case(h, case, "fp32", kernel="simt")
+
+
+def test_simt_kat_integer_pattern_tn(h):
+    """The reference's own fixture (TN, padding 64, alpha 0.314, beta 0.2718) at 768x640x256."""
+    import torch
+    M, N, K = 768, 640, 256
+    A, B, C, lda, ldb, ldc = gg.kat_case(M, N, K, 64)
+    dA, dB, dC = (torch.from_numpy(x).cuda() for x in (A, B, C))
+    D = torch.zeros(ldc * N, dtype=torch.float32, device="cuda")
+    p = tl.Problem.make(M, N, K, dtype="fp32", trans_a=True, alpha=float(gg.ALPHA_KAT), beta=float(gg.BETA_KAT),
+                        lda=lda, ldb=ldb, ldc=ldc, ldd=ldc, kernel="simt")
+    h.gemm(p, D, dC, dA, dB)
+    got = gu.mat(D.cpu().numpy(), M, N, ldc)
+    exp = gu.mat(gg.kat_expected(M, N, K, 64), M, N, ldc)
+    # integer sums are exact on both sides; only the final alpha/beta step may differ by one ulp (fma)
+    assert gu.ulp_diff_count(got, exp, "fp32") == 0
+
+
+# ---------------------------------------------------------------------------- tcgen05 kernel
+@pytest.mark.parametrize("dt", ["bf16", "fp16"])
+@pytest.mark.parametrize("lay", ["TN", "NN", "NT", "TT"])
+def test_tc_small_golden(h, dt, lay):
+    """Small seeded cases; the oracle's output is also a committed golden fixture."""
+    gold = np.load(os.path.join(GOLD, "gemm_small.npz"))
+    seed = 1000 + gg.DTYPES.index(dt) * 10 + gg.LAYOUTS.index(lay)
+    case = gg.make_case(dt, lay, seed, **gg.SMALL)
+    assert np.array_equal(gu.oracle_ref(case).view(np.uint32), gold[f"{dt}_{lay}"])
+    check_case(h, case, dt, kernel="tcgen05")
+
+
+@pytest.mark.parametrize("dt", ["bf16", "fp16"])
+@pytest.mark.parametrize("lay", ["TN", "NN", "NT", "TT"])
+@pytest.mark.parametrize("mnk", [(256, 384, 320), (130, 200, 72), (480, 1024, 256), (64, 64, 64), (1, 1, 64),
+                                 (300, 129, 1000)])
+def test_tc_layouts_sizes(h, dt, lay, mnk):
+    m, n, k = mnk
+    seed = 7 + m + 3 * n + k
+    case = gg.make_case(dt, lay, seed, m, n, k)
+    check_case(h, case, dt, kernel="tcgen05")
+
+
+@pytest.mark.parametrize("bm", [64, 128, 192, 256])
+@pytest.mark.parametrize("stages", [2, 4])
+@pytest.mark.parametrize("split", [1, 3])
+def test_tc_solutions(h, bm, stages, split):
+    case = gg.make_case("bf16", "NN", 99, 333, 300, 640)
+    sol = tl.Solution(kernel=tl.KERNEL_TCGEN05, macro_tile0=bm, macro_tile1=128, depth_u=64, stages=stages,
+                      split_k=split, raster=4)
+    check_case(h, case, "bf16", kernel="tcgen05", solution=sol)
+
+
+def test_tc_fp32_output_and_truncation(h):
+    case = gg.make_case("bf16", "TN", 5, 200, 160, 512)
+    got = gu.run_case(h, case, kernel="tcgen05", dtype="bf16", out_dtype="fp32")
+    # fp32 output of a bf16 GEMM: compare with the oracle's fp32 loop on the same (exact) inputs
+    c2 = dict(case)
+    c2["C"] = case["C"]
+    ref = gu.mat(gu.oracle_ref(c2), 200, 160, 200)
+    assert orc.normwise_error(gu.mat(got, 200, 160, 200), ref) <= fp32_tol(512)
+    # reference bf16 store mode: truncation (src/gemmMfmaKernelWriter.h:1661-1665)
+    check_case(h, case, "bf16", kernel="tcgen05", rounding="trunc")
+
+
+def test_tc_batched(h):
+    import torch
+    m, n, k, batch = 96, 130, 192, 3
+    g = np.random.default_rng(17)
+    A = orc.encode(g.standard_normal(m * k * batch).astype(np.float32), "bf16")
+    B = orc.encode(g.standard_normal(k * n * batch).astype(np.float32), "bf16")
+    C = orc.encode(g.standard_normal(m * n * batch).astype(np.float32), "bf16")
+    Af, Bf, Cf = (orc.decode(x, "bf16") for x in (A, B, C))
+    dA, dB, dC = gu.to_dev(A, "bf16"), gu.to_dev(B, "bf16"), gu.to_dev(C, "bf16")
+    dD = torch.empty(m * n * batch, dtype=torch.bfloat16, device="cuda")
+    p = tl.Problem.make(m, n, k, dtype="bf16", alpha=1.5, beta=-0.5, batch=batch, kernel="tcgen05")
+    h.gemm(p, dD, dC, dA, dB)
+    got = gu.from_dev(dD, "bf16")
+    ref = orc.gemm_ref_f32(0, 0, m, n, k, 1.5, Af, m, Bf, k, -0.5, Cf, m, m, batch=batch, stride_a=m * k,
+                           stride_b=k * n, stride_c=m * n, stride_d=m * n)
+    assert gu.ulp_diff_count(got, gu.quantize_out(ref, "bf16"), "bf16") == 0
+
+
+def test_tc_in_place_beta_and_k0(h):
+    import torch
+    case = gg.make_case("fp16", "TN", 3, 128, 128, 128)
+    C = gu.to_dev(case["C_bits"], "fp16")
+    D = C.clone()
+    p = tl.Problem.make(128, 128, 128, dtype="fp16", trans_a=True, alpha=1.0, beta=0.5, kernel="tcgen05")
+    A, B = gu.to_dev(case["A_bits"], "fp16"), gu.to_dev(case["B_bits"], "fp16")
+    h.gemm(p, D, D, A, B)        # D == C in place
+    ref = gu.quantize_out(gu.oracle_ref(case), "fp16")
+    assert gu.ulp_diff_count(gu.from_dev(D, "fp16"), ref, "fp16") == 0
+    # k == 0: D = beta * C
+    p0 = tl.Problem.make(128, 128, 0, dtype="fp16", trans_a=True, alpha=1.0, beta=0.5, lda=1, kernel="tcgen05")
+    D0 = torch.empty_like(C)
+    h.gemm(p0, D0, C, A, B)
+    exp = gu.quantize_out(0.5 * case["C"], "fp16")
+    assert np.array_equal(gu.from_dev(D0, "fp16"), exp)
+
+
+def test_unaligned_ld_falls_back_to_simt(h):
+    """lda*2 bytes not a multiple of 16: TMA cannot describe it; AUTO routes to the CUDA-core kernel,
+    an explicit TCGEN05 request is refused."""
+    case = gg.make_case("bf16", "NN", 4, 61, 33, 47)      # lda = 61, ldb = 47
+    check_case(h, case, "bf16", kernel="auto")
+    with pytest.raises(tl.TLError) as e:
+        gu.run_case(h, case, kernel="tcgen05", dtype="bf16")
+    assert e.value.status == tl.ERR_UNSUPPORTED
+
+
+# ---------------------------------------------------------------------------- bf16x3 and fp8
+def test_bf16x3_accuracy_beats_fp32_simt(h):
+    import torch
+    g = orc.rng(2)
+    M = N = K = 1024
+    A = orc.uniform_pm1(g, M * K).astype(np.float32)
+    B = orc.uniform_pm1(g, K * N).astype(np.float32)
+    dA, dB = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+    ref, absprod = orc.gemm_f64_numpy(False, False, M, N, K, 1.0, A, M, B, K)
+    errs = {}
+    for kern in ("bf16x3", "simt"):
+        D = torch.empty(M * N, dtype=torch.float32, device="cuda")
+        h.gemm(tl.Problem.make(M, N, K, dtype="fp32", kernel=kern), D, None, dA, dB)
+        got = gu.mat(D.cpu().numpy(), M, N, M)
+        errs[kern] = orc.normwise_error(got, ref)
+        assert orc.componentwise_error(got, ref, absprod) < 1e-6
+    assert errs["bf16x3"] < 2e-6, errs
+
+
+def test_split_bf16x2_exact(h):
+    import torch
+    g = np.random.default_rng(8)
+    x = (g.standard_normal(10001) * 10).astype(np.float32)
+    dx = torch.from_numpy(x).cuda()
+    hi = torch.empty(x.size, dtype=torch.bfloat16, device="cuda")
+    lo = torch.empty_like(hi)
+    h.split_bf16x2(dx, x.size, hi, lo)
+    hb = gu.from_dev(hi, "bf16")
+    lb = gu.from_dev(lo, "bf16")
+    assert np.array_equal(hb, orc.decode(orc.f32_to_bf16(x), "bf16"))
+    assert np.array_equal(lb, orc.decode(orc.f32_to_bf16(x - hb), "bf16"))
+
+
+def test_fp8_quantize_bit_exact(h):
+    import torch
+    g = np.random.default_rng(12)
+    x = g.standard_normal(50000).astype(np.float32)
+    dx = torch.from_numpy(x).cuda()
+    q = torch.empty(x.size, dtype=torch.uint8, device="cuda")
+    scale = torch.zeros(1, dtype=torch.float32, device="cuda")
+    amax = torch.zeros(1, dtype=torch.float32, device="cuda")
+    h.quantize_fp8(dx, x.size, q, scale_out=scale, amax_out=amax)
+    a = np.float32(np.max(np.abs(x)))
+    s = np.float32(448.0) / a
+    assert amax.item() == a
+    assert scale.item() == np.float32(a / np.float32(448.0))
+    assert np.array_equal(q.cpu().numpy(), orc.f32_to_e4m3((x * s).astype(np.float32)))
+
+
+@pytest.mark.parametrize("lay", ["TN", "NN", "NT", "TT"])
+def test_fp8_gemm(h, lay):
+    case = gg.make_case("fp8", lay, 31 + gg.LAYOUTS.index(lay), 256, 200, 384)
+    check_case(h, case, "fp8", kernel="tcgen05")
+    # with dequantisation scales folded into alpha
+    got = gu.run_case(h, case, kernel="tcgen05", dtype="fp8", scale_a=0.5, scale_b=0.25)
+    c2 = dict(case)
+    c2["alpha"] = case["alpha"] * 0.125
+    ref = gu.quantize_out(gu.oracle_ref(c2), "bf16")
+    assert gu.ulp_diff_count(got, ref, "bf16") == 0
+
+
+# ---------------------------------------------------------------------------- grouped + graphs
+def _grouped_setup(count, seed, dt="bf16", lay="NN"):
+    import torch
+    g = np.random.default_rng(seed)
+    probs, cases, D, C, A, B = [], [], [], [], [], []
+    for i in range(count):
+        m = int(16 * g.integers(1, 20))
+        n = int(16 * g.integers(1, 20))
+        k = int(64 * g.integers(1, 8))
+        case = gg.make_case(dt, lay, seed * 1000 + i, m, n, k, alpha=1.0, beta=0.5 if i % 2 else 0.0)
+        cases.append(case)
+        A.append(gu.to_dev(case["A_bits"], dt))
+        B.append(gu.to_dev(case["B_bits"], dt))
+        C.append(gu.to_dev(case["C_bits"], case["out_dtype"]))
+        D.append(torch.full((m * n,), float("nan"), dtype=gu.torch_dtype(case["out_dtype"]), device="cuda"))
+        probs.append(tl.Problem.make(m, n, k, dtype=dt, out_dtype=case["out_dtype"], trans_a=case["trans_a"],
+                                     trans_b=case["trans_b"], alpha=case["alpha"], beta=case["beta"], lda=case["lda"],
+                                     ldb=case["ldb"], ldc=m, ldd=m, kernel="tcgen05"))
+    return probs, cases, D, C, A, B
+
+
+def _check_grouped(cases, D):
+    for case, d in zip(cases, D):
+        got = gu.from_dev(d, case["out_dtype"])
+        ref = gu.quantize_out(gu.oracle_ref(case), case["out_dtype"])
+        assert gu.ulp_diff_count(got, ref, case["out_dtype"]) == 0
+
+
+@pytest.mark.parametrize("lay", ["NN", "TN"])
+def test_grouped_one_launch(h, lay):
+    probs, cases, D, C, A, B = _grouped_setup(24, 5, lay=lay)
+    n0 = h.launch_count()
+    plan = h.grouped_plan(probs, D, C, A, B)
+    plan.launch()
+    h.device_status()
+    assert h.launch_count() - n0 == 1
+    _check_grouped(cases, D)
+    plan.close()
+
+
+def test_grouped_graph_replay(h):
+    import torch
+    probs, cases, D, C, A, B = _grouped_setup(12, 9)
+    plan = h.grouped_plan(probs, D, C, A, B)
+    s = torch.cuda.Stream()
+    graph = plan.capture(s)
+    for d in D:
+        d.fill_(float("nan"))
+    torch.cuda.synchronize()
+    graph.launch(s)
+    graph.launch(s)
+    s.synchronize()
+    h.device_status()
+    _check_grouped(cases, D)
+    graph.close()
+    plan.close()
+
+
+def test_gemm_graph_capture(h):
+    import torch
+    case = gg.make_case("bf16", "NT", 77, 512, 256, 512)
+    A, B = gu.to_dev(case["A_bits"], "bf16"), gu.to_dev(case["B_bits"], "bf16")
+    C = gu.to_dev(case["C_bits"], "bf16")
+    D = torch.empty(512 * 256, dtype=torch.bfloat16, device="cuda")
+    p = tl.Problem.make(512, 256, 512, dtype="bf16", trans_b=True, alpha=1.0, beta=0.5, lda=case["lda"],
+                        ldb=case["ldb"], kernel="tcgen05")
+    s = torch.cuda.Stream()
+    graph = h.capture_gemm(p, D, C, A, B, stream=s)
+    graph.launch(s)
+    s.synchronize()
+    ref = gu.quantize_out(gu.oracle_ref(case), "bf16")
+    assert gu.ulp_diff_count(gu.from_dev(D, "bf16"), ref, "bf16") == 0
+    graph.close()
+
+
+# ---------------------------------------------------------------------------- tuner, norms, autograd
+def test_tune_and_cache(h, tmp_path):
+    import torch
+    case = gg.make_case("bf16", "NN", 55, 480, 1024, 1024)
+    A, B = gu.to_dev(case["A_bits"], "bf16"), gu.to_dev(case["B_bits"], "bf16")
+    D = torch.empty(480 * 1024, dtype=torch.bfloat16, device="cuda")
+    p = tl.Problem.make(480, 1024, 1024, dtype="bf16", kernel="tcgen05")
+    path = str(tmp_path / "tuned.json")
+    sol, ms = h.tune(p, D, None, A, B, max_candidates=6, reps=3, cache_path=path)
+    assert ms > 0
+    h.check_solution(p, sol)
+    h2 = tl.Handle()
+    assert h2.load_solutions(path) == 1
+    c = dict(case)
+    c["beta"] = 0.0
+    check_case(h2, c, "bf16", kernel="tcgen05")
+    h2.close()
+
+
+def test_error_norms_device(h):
+    import torch
+    g = np.random.default_rng(1)
+    m, n = 300, 200
+    R = g.standard_normal(m * n)
+    Dv = (R + g.standard_normal(m * n) * 1e-3).astype(np.float32)
+    W = np.abs(g.standard_normal(m * n)) + 0.5
+    out = h.error_norms(tl.FP32, torch.from_numpy(Dv).cuda(), m, torch.from_numpy(R).cuda(), m, m, n,
+                        W=torch.from_numpy(W).cuda())
+    diff = np.abs(Dv.astype(np.float64) - R)
+    assert out[0] == pytest.approx(diff.max(), rel=0, abs=0)
+    assert out[1] == pytest.approx(np.abs(R).max(), rel=0, abs=0)
+    assert out[2] == pytest.approx((diff / W).max(), rel=1e-15)
+
+
+def test_autograd_finite_differences_fp64():
+    """Y = X W at M=64, K=48, N=32 (bf16 kernels); gradients vs central differences of the fp64
+    function, relative error below 1e-2."""
+    import torch
+    g = torch.Generator().manual_seed(4)
+    M, K, N = 64, 48, 32
+    X64 = torch.randn(M, K, generator=g, dtype=torch.float64) * 0.02 * 50
+    W64 = torch.randn(K, N, generator=g, dtype=torch.float64) * 0.02 * 50
+    dY = torch.randn(M, N, generator=g, dtype=torch.float64)
+    Xb = X64.to(torch.bfloat16).cuda().requires_grad_()
+    Wb = W64.to(torch.bfloat16).cuda().requires_grad_()
+    Y = tl.matmul(Xb, Wb)
+    Y.backward(dY.to(torch.bfloat16).cuda())
+    Xe, We = Xb.detach().double().cpu(), Wb.detach().double().cpu()
+    dYe = dY.to(torch.bfloat16).double()
+
+    def loss(X, W):
+        return float((X @ W * dYe).sum())
+
+    eps = 1e-3
+    for name, T, grad in (("X", Xe, Xb.grad), ("W", We, Wb.grad)):
+        gnum = torch.zeros_like(T)
+        for i in range(T.shape[0]):
+            for j in range(T.shape[1]):
+                Tp, Tm = T.clone(), T.clone()
+                Tp[i, j] += eps
+                Tm[i, j] -= eps
+                gnum[i, j] = (loss(Tp, We) - loss(Tm, We)) / (2 * eps) if name == "X" else \
+                    (loss(Xe, Tp) - loss(Xe, Tm)) / (2 * eps)
+        ga = grad.double().cpu()
+        rel = float((ga - gnum).abs().max() / gnum.abs().max())
+        assert rel < 1e-2, (name, rel)
+
+
+def test_autograd_layouts_match_fp64_gradient():
+    import torch
+    g = torch.Generator().manual_seed(4)
+    M, K, N = 512, 256, 384
+    X = (torch.randn(M, K, generator=g) * 0.02).to(torch.bfloat16).cuda().requires_grad_()
+    W = (torch.randn(K, N, generator=g) * 0.02).to(torch.bfloat16).cuda().requires_grad_()
+    dY = torch.randn(M, N, generator=g).to(torch.bfloat16).cuda()
+    Y = tl.matmul(X, W)
+    Y.backward(dY)
+    Xd, Wd, dYd = X.detach().double(), W.detach().double(), dY.double()
+    for got, ref in ((Y, Xd @ Wd), (X.grad, dYd @ Wd.T), (W.grad, Xd.T @ dYd)):
+        rel = float((got.double() - ref).abs().max() / ref.abs().max())
+        assert rel < 1e-2
