@@ -69,7 +69,9 @@ typedef enum tl_kernel {
     TL_KERNEL_AUTO = 0,     /* fp32 -> SIMT, fp16/bf16/fp8 -> TCGEN05 */
     TL_KERNEL_SIMT = 1,     /* CUDA-core FMA kernel, any input type, fp32 accumulation */
     TL_KERNEL_TCGEN05 = 2,  /* TMA -> smem ring -> tcgen05.mma (TMEM accumulator) -> epilogue */
-    TL_KERNEL_BF16X3 = 3    /* fp32 inputs split hi/lo into bf16, 3 tensor-core products */
+    TL_KERNEL_BF16X3 = 3,   /* fp32 inputs split hi/lo into bf16, 3 tensor-core products */
+    TL_KERNEL_BF16X6 = 4    /* fp32 inputs split into 3 bf16 pieces, 6 tensor-core products
+                               (the terms of order <= 2^-16); FP32-class accuracy */
 } tl_kernel;
 
 /* Rounding of fp32 results into fp16/bf16 outputs.  TRUNCATE reproduces the reference's bf16

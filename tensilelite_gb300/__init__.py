@@ -31,12 +31,13 @@ ERR_INVALID_ARG, ERR_UNSUPPORTED, ERR_TIMEOUT, ERR_CUDA, ERR_ALLOC = 16, 17, 18,
 # dtype codes: 1..3 are the reference's -d codes
 FP32, FP16, BF16, FP8 = 1, 2, 3, 4
 OP_N, OP_T = 0, 1
-KERNEL_AUTO, KERNEL_SIMT, KERNEL_TCGEN05, KERNEL_BF16X3 = 0, 1, 2, 3
+KERNEL_AUTO, KERNEL_SIMT, KERNEL_TCGEN05, KERNEL_BF16X3, KERNEL_BF16X6 = 0, 1, 2, 3, 4
 ROUND_RNE, ROUND_TRUNCATE = 0, 1
 
 DTYPE_BYTES = {FP32: 4, FP16: 2, BF16: 2, FP8: 1}
 DTYPE_NAMES = {"fp32": FP32, "fp16": FP16, "bf16": BF16, "fp8": FP8, "fp8_e4m3": FP8}
-KERNEL_NAMES = {"auto": KERNEL_AUTO, "simt": KERNEL_SIMT, "tcgen05": KERNEL_TCGEN05, "bf16x3": KERNEL_BF16X3}
+KERNEL_NAMES = {"auto": KERNEL_AUTO, "simt": KERNEL_SIMT, "tcgen05": KERNEL_TCGEN05, "bf16x3": KERNEL_BF16X3,
+                "bf16x6": KERNEL_BF16X6}
 
 
 class TLError(RuntimeError):

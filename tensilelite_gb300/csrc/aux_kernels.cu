@@ -1,5 +1,5 @@
 // aux_kernels.cu -- the memory-bound helpers around the GEMM:
-//   split_bf16x2     fp32 -> (hi, lo) bf16 pair for the bf16x3 FP32-accurate product
+//   split_bf16       fp32 -> 2 or 3 bf16 pieces for the FP32-accurate bf16x3 / bf16x6 products
 //   amax / quant     per-tensor amax and E4M3 quantisation (scale = 448 / amax)
 //   error_norms      FP64 reduction of max|d - r|, max|r| and the componentwise ratio
 //   fill_pattern     the reference's deterministic InitRealData codes, on the device
@@ -55,38 +55,54 @@ __device__ __forceinline__ void store_from_float(int dtype, int trunc, void* p, 
     }
 }
 
-// ---- bf16x3 split ------------------------------------------------------------------------------------
-__device__ __forceinline__ void split1(float x, uint16_t& h, uint16_t& l)
+// ---- split-precision pieces -------------------------------------------------------------------------
+// p0 = bf16(x), p1 = bf16(x - p0), p2 = bf16(x - p0 - p1); every subtraction is exact in fp32 (the
+// residual of a rounding is representable), so x = p0 + p1 + p2 + O(2^-24 |x|).
+template <int NP>
+__device__ __forceinline__ void split_pieces(float x, uint16_t (&o)[3])
 {
-    const __nv_bfloat16 hb = __float2bfloat16_rn(x);
-    const float r = x - __bfloat162float(hb);          // exact in fp32
-    const __nv_bfloat16 lb = __float2bfloat16_rn(r);
-    h = __bfloat16_as_ushort(hb);
-    l = __bfloat16_as_ushort(lb);
+    float r = x;
+#pragma unroll
+    for (int i = 0; i < NP; ++i) {
+        const __nv_bfloat16 b = __float2bfloat16_rn(r);
+        o[i] = __bfloat16_as_ushort(b);
+        r = r - __bfloat162float(b);
+    }
 }
 
+template <int NP>
 __global__ void split_kernel(const float* __restrict__ src, int64_t rows, int64_t cols, int64_t ld, int64_t batch,
-                             int64_t bs, uint16_t* __restrict__ hi, uint16_t* __restrict__ lo)
+                             int64_t bs, uint16_t* __restrict__ p0, uint16_t* __restrict__ p1,
+                             uint16_t* __restrict__ p2)
 {
     // element e of the logical rows x cols x batch block lives at b*bs + c*ld + r
     const int64_t total = rows * cols * batch;
     const bool dense = (ld == rows) && (batch == 1 || bs == rows * cols);
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    if (dense && (reinterpret_cast<uintptr_t>(src) & 15) == 0 && (reinterpret_cast<uintptr_t>(hi) & 7) == 0 &&
-        (reinterpret_cast<uintptr_t>(lo) & 7) == 0) {
+    uint16_t* out[3] = {p0, p1, p2};
+    bool vec = dense && (reinterpret_cast<uintptr_t>(src) & 15) == 0;
+#pragma unroll
+    for (int i = 0; i < NP; ++i) vec = vec && (reinterpret_cast<uintptr_t>(out[i]) & 7) == 0;
+    if (vec) {
         const int64_t n4 = total / 4;
         for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n4; i += stride) {
             const float4 v = reinterpret_cast<const float4*>(src)[i];
-            uint16_t h[4], l[4];
-            split1(v.x, h[0], l[0]);
-            split1(v.y, h[1], l[1]);
-            split1(v.z, h[2], l[2]);
-            split1(v.w, h[3], l[3]);
-            reinterpret_cast<uint2*>(hi)[i] = make_uint2(h[0] | (uint32_t(h[1]) << 16), h[2] | (uint32_t(h[3]) << 16));
-            reinterpret_cast<uint2*>(lo)[i] = make_uint2(l[0] | (uint32_t(l[1]) << 16), l[2] | (uint32_t(l[3]) << 16));
+            uint16_t q[4][3];
+            split_pieces<NP>(v.x, q[0]);
+            split_pieces<NP>(v.y, q[1]);
+            split_pieces<NP>(v.z, q[2]);
+            split_pieces<NP>(v.w, q[3]);
+#pragma unroll
+            for (int pc = 0; pc < NP; ++pc)
+                reinterpret_cast<uint2*>(out[pc])[i] = make_uint2(q[0][pc] | (uint32_t(q[1][pc]) << 16),
+                                                                  q[2][pc] | (uint32_t(q[3][pc]) << 16));
         }
-        for (int64_t i = n4 * 4 + blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total; i += stride)
-            split1(src[i], hi[i], lo[i]);
+        for (int64_t i = n4 * 4 + blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total; i += stride) {
+            uint16_t q[3];
+            split_pieces<NP>(src[i], q);
+#pragma unroll
+            for (int pc = 0; pc < NP; ++pc) out[pc][i] = q[pc];
+        }
         return;
     }
     for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < total; e += stride) {
@@ -94,7 +110,10 @@ __global__ void split_kernel(const float* __restrict__ src, int64_t rows, int64_
         const int64_t c = (e / rows) % cols;
         const int64_t b = e / (rows * cols);
         const int64_t off = b * bs + c * ld + r;
-        split1(src[off], hi[off], lo[off]);
+        uint16_t q[3];
+        split_pieces<NP>(src[off], q);
+#pragma unroll
+        for (int pc = 0; pc < NP; ++pc) out[pc][off] = q[pc];
     }
 }
 
@@ -215,12 +234,15 @@ tl_status check_launch(const char* what, int64_t* launches)
 
 }  // namespace
 
-tl_status aux_split_bf16x2(const float* src, int64_t rows, int64_t cols, int64_t ld, int64_t batch,
-                           int64_t batch_stride, uint16_t* hi, uint16_t* lo, cudaStream_t s, int64_t* launches)
+tl_status aux_split_bf16(const float* src, int64_t rows, int64_t cols, int64_t ld, int64_t batch,
+                         int64_t batch_stride, uint16_t* p0, uint16_t* p1, uint16_t* p2, cudaStream_t s,
+                         int64_t* launches)
 {
     const int64_t total = rows * cols * batch;
     if (total == 0) return TL_SUCCESS;
-    split_kernel<<<grid_for(total, 8, 256), 256, 0, s>>>(src, rows, cols, ld, batch, batch_stride, hi, lo);
+    const int grid = grid_for(total, 8, 256);
+    if (p2) split_kernel<3><<<grid, 256, 0, s>>>(src, rows, cols, ld, batch, batch_stride, p0, p1, p2);
+    else split_kernel<2><<<grid, 256, 0, s>>>(src, rows, cols, ld, batch, batch_stride, p0, p1, nullptr);
     return check_launch("split_kernel", launches);
 }
 

@@ -39,7 +39,7 @@ namespace tl {
 namespace {
 
 struct TcKernelParams {
-    CUtensorMap tmN, tmM, tmN_lo, tmM_lo;
+    CUtensorMap tmN[3], tmM[3];   // split-precision pieces 0..2 (piece 0 = the operand itself)
     const TcGroupEntry* group;
     const int64_t* group_prefix;
     int group_count;
@@ -48,7 +48,9 @@ struct TcKernelParams {
     int64_t ldd, ldc, stride_d, stride_c;
     int M, N, K, batch;
     float alpha, beta;
-    int bm, stages, split_k, raster, x3;
+    int bm, stages, split_k, raster;
+    int nterms;                   // tensor-core products per k-block (1, or 3 / 6 for the fp32 split)
+    uint8_t term_n[8], term_m[8]; // piece of B / of A used by each product
     int tiles_m, tiles_n;
     int64_t total_work;
     int num_kb;
@@ -66,8 +68,6 @@ struct TcKernelParams {
 struct TileJob {
     const void* tmN;
     const void* tmM;
-    const void* tmN_lo;
-    const void* tmM_lo;
     void* D;
     const void* C;
     int64_t ldd, ldc;
@@ -100,10 +100,8 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, Tile
             in = static_cast<int>(t / p.tiles_m);
             jm = static_cast<int>(t % p.tiles_m);
         }
-        j.tmN = &p.tmN;
-        j.tmM = &p.tmM;
-        j.tmN_lo = &p.tmN_lo;
-        j.tmM_lo = &p.tmM_lo;
+        j.tmN = &p.tmN[0];
+        j.tmM = &p.tmM[0];
         j.D = static_cast<char*>(p.D);
         j.C = p.C;
         j.ldd = p.ldd;
@@ -132,8 +130,6 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, Tile
         const int jm = static_cast<int>(t % e.tiles_m);
         j.tmN = &e.tmN;
         j.tmM = &e.tmM;
-        j.tmN_lo = &e.tmN;
-        j.tmM_lo = &e.tmM;
         j.D = e.D;
         j.C = e.C;
         j.ldd = e.ldd;
@@ -311,18 +307,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
         ptx::tmem_relinquish();
     }
     if (warp == 0 && lane == 0 && p.group == nullptr) {
-        ptx::prefetch_tmap(&p.tmN);
-        ptx::prefetch_tmap(&p.tmM);
-        if (p.x3) {
-            ptx::prefetch_tmap(&p.tmN_lo);
-            ptx::prefetch_tmap(&p.tmM_lo);
+        for (int v = 0; v < p.nterms; ++v) {
+            ptx::prefetch_tmap(&p.tmN[p.term_n[v]]);
+            ptx::prefetch_tmap(&p.tmM[p.term_m[v]]);
         }
     }
     ptx::tc_fence_before();
     __syncthreads();
     ptx::tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
-    const int nvirt = p.x3 ? 3 : 1;
+    const int nvirt = p.nterms;
     const uint64_t tlim = p.timeout_ns;
 
     if (warp == 0) {
@@ -343,9 +337,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         }
                         uint8_t* sN = smem + static_cast<size_t>(stage) * stage_bytes;
                         uint8_t* sM = sN + tileN_bytes;
-                        // bf16x3 order per k-block: (B_lo, A_hi), (B_hi, A_lo), (B_hi, A_hi)
-                        const void* mapN = (p.x3 && v == 0) ? j.tmN_lo : j.tmN;
-                        const void* mapM = (p.x3 && v == 1) ? j.tmM_lo : j.tmM;
+                        // split-precision products, smallest first (term table set by the host)
+                        const void* mapN = p.group ? j.tmN : static_cast<const void*>(&p.tmN[p.term_n[v]]);
+                        const void* mapM = p.group ? j.tmM : static_cast<const void*>(&p.tmM[p.term_m[v]]);
                         ptx::mbar_arrive_expect_tx(&full[stage], stage_bytes);
                         const int k0 = kb * W;
                         if (!p.n_mn_major) {
@@ -660,12 +654,18 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     TcKernelParams kp;
     memset(&kp, 0, sizeof(kp));
     tl_status st;
-    if ((st = tc_encode_operand(&kp.tmN, L.in_dtype, L.opN, L.K, L.batch, kTcTileN)) != TL_SUCCESS) return st;
-    if ((st = tc_encode_operand(&kp.tmM, L.in_dtype, L.opM, L.K, L.batch, L.bm)) != TL_SUCCESS) return st;
-    if (L.x3) {
-        if ((st = tc_encode_operand(&kp.tmN_lo, L.in_dtype, L.opN_lo, L.K, L.batch, kTcTileN)) != TL_SUCCESS) return st;
-        if ((st = tc_encode_operand(&kp.tmM_lo, L.in_dtype, L.opM_lo, L.K, L.batch, L.bm)) != TL_SUCCESS) return st;
+    const int pieces = L.pieces < 1 ? 1 : L.pieces;
+    for (int i = 0; i < pieces; ++i) {
+        if ((st = tc_encode_operand(&kp.tmN[i], L.in_dtype, L.opN[i], L.K, L.batch, kTcTileN)) != TL_SUCCESS) return st;
+        if ((st = tc_encode_operand(&kp.tmM[i], L.in_dtype, L.opM[i], L.K, L.batch, L.bm)) != TL_SUCCESS) return st;
     }
+    // products per k-block, smallest first: 2-piece split -> A1B0, A0B1, A0B0;
+    // 3-piece split -> A2B0, A1B1, A0B2, A1B0, A0B1, A0B0
+    static const uint8_t t3m[3] = {1, 0, 0}, t3n[3] = {0, 1, 0};
+    static const uint8_t t6m[6] = {2, 1, 0, 1, 0, 0}, t6n[6] = {0, 1, 2, 0, 1, 0};
+    if (pieces == 1) { kp.nterms = 1; kp.term_m[0] = kp.term_n[0] = 0; }
+    else if (pieces == 2) { kp.nterms = 3; for (int i = 0; i < 3; ++i) { kp.term_m[i] = t3m[i]; kp.term_n[i] = t3n[i]; } }
+    else { kp.nterms = 6; for (int i = 0; i < 6; ++i) { kp.term_m[i] = t6m[i]; kp.term_n[i] = t6n[i]; } }
     const int W = kTcRowBytes / dtype_bytes(L.in_dtype);
     kp.group = nullptr;
     kp.D = L.D;
@@ -684,14 +684,13 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     kp.stages = L.stages;
     kp.split_k = L.split_k;
     kp.raster = L.raster;
-    kp.x3 = L.x3;
     kp.tiles_m = static_cast<int>((L.M + L.bm - 1) / L.bm);
     kp.tiles_n = static_cast<int>((L.N + kTcTileN - 1) / kTcTileN);
     kp.num_kb = static_cast<int>((L.K + W - 1) / W);
     kp.kb_elems = W;
     kp.total_work = static_cast<int64_t>(kp.tiles_m) * kp.tiles_n * L.batch * L.split_k;
-    kp.n_mn_major = L.opN.mn_major;
-    kp.m_mn_major = L.opM.mn_major;
+    kp.n_mn_major = L.opN[0].mn_major;
+    kp.m_mn_major = L.opM[0].mn_major;
     kp.idesc = make_idesc(L.in_dtype, kp.n_mn_major, kp.m_mn_major, L.bm);
     desc_params(L.in_dtype, kp.n_mn_major, kp.n_lbo, kp.n_kstep);
     desc_params(L.in_dtype, kp.m_mn_major, kp.m_lbo, kp.m_kstep);
@@ -719,7 +718,7 @@ tl_status tc_grouped_launch(const TcGroupLaunch& G, cudaStream_t stream, int64_t
     kp.bm = G.bm;
     kp.stages = G.stages;
     kp.split_k = 1;
-    kp.x3 = 0;
+    kp.nterms = 1;
     kp.total_work = G.total_tiles;
     kp.kb_elems = kTcRowBytes / dtype_bytes(G.in_dtype);
     kp.stride_c = 0;

@@ -82,6 +82,9 @@ cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
+bool is_split(int kernel) { return kernel == TL_KERNEL_BF16X3 || kernel == TL_KERNEL_BF16X6; }
+int split_pieces(int kernel) { return kernel == TL_KERNEL_BF16X6 ? 3 : (kernel == TL_KERNEL_BF16X3 ? 2 : 1); }
+
 std::string dims_str(const tl_gemm_problem& p)
 {
     char buf[200];
@@ -113,9 +116,9 @@ tl_status validate(const tl_gemm_problem* p)
     if (p->ldb < std::max<int64_t>(1, b_rows)) return fail(TL_ERR_INVALID_ARG, "ldb smaller than op(B) storage rows");
     if (p->ldd < std::max<int64_t>(1, p->m)) return fail(TL_ERR_INVALID_ARG, "ldd < m");
     if (p->beta != 0.0f && p->ldc < std::max<int64_t>(1, p->m)) return fail(TL_ERR_INVALID_ARG, "ldc < m");
-    if (p->kernel < TL_KERNEL_AUTO || p->kernel > TL_KERNEL_BF16X3) return fail(TL_ERR_INVALID_ARG, "bad kernel id");
-    if (p->kernel == TL_KERNEL_BF16X3 && p->dtype_a != TL_DTYPE_FP32)
-        return fail(TL_ERR_UNSUPPORTED, "bf16x3 needs fp32 inputs");
+    if (p->kernel < TL_KERNEL_AUTO || p->kernel > TL_KERNEL_BF16X6) return fail(TL_ERR_INVALID_ARG, "bad kernel id");
+    if ((p->kernel == TL_KERNEL_BF16X3 || p->kernel == TL_KERNEL_BF16X6) && p->dtype_a != TL_DTYPE_FP32)
+        return fail(TL_ERR_UNSUPPORTED, "bf16x3/bf16x6 need fp32 inputs");
     if (p->kernel == TL_KERNEL_TCGEN05 && p->dtype_a == TL_DTYPE_FP32)
         return fail(TL_ERR_UNSUPPORTED, "the tcgen05 kernel takes fp16/bf16/fp8 inputs (use BF16X3 for fp32)");
     if (p->out_rounding != TL_ROUND_RNE && p->out_rounding != TL_ROUND_TRUNCATE)
@@ -134,7 +137,7 @@ bool tma_ok(const tl_gemm_problem& p, const void* A, const void* B, std::string*
 {
     const int es = dtype_bytes(p.dtype_a);
     auto bad = [&](const char* w) { if (why) *why = w; return false; };
-    if (p.kernel == TL_KERNEL_BF16X3) return true;   // operands are re-laid into the workspace
+    if (is_split(p.kernel)) return true;   // operands are re-laid into the workspace
     if (!aligned16(A) || !aligned16(B)) return bad("A/B not 16-byte aligned");
     if ((p.lda * es) % 16 || (p.ldb * es) % 16) return bad("lda/ldb not a multiple of 16 bytes");
     if (p.batch > 1 && (((p.stride_a * es) % 16) || ((p.stride_b * es) % 16)))
@@ -175,9 +178,9 @@ void tc_heuristic(const tl_handle* h, const tl_gemm_problem& p, int kernel, tl_g
 {
     memset(s, 0, sizeof(*s));
     s->kernel = kernel;
-    const int in = (kernel == TL_KERNEL_BF16X3) ? TL_DTYPE_BF16 : p.dtype_a;
+    const int in = is_split(kernel) ? TL_DTYPE_BF16 : p.dtype_a;
     const int W = row_elems(in);
-    const bool mmn = (kernel == TL_KERNEL_BF16X3) ? false : m_mn_major(p);
+    const bool mmn = m_mn_major(p);
     const int64_t tiles_n = (p.n + kTcTileN - 1) / kTcTileN;
     const int64_t num_kb = (p.k + W - 1) / W;
     int bm = 256;
@@ -209,7 +212,7 @@ void tc_heuristic(const tl_handle* h, const tl_gemm_problem& p, int kernel, tl_g
 
 tl_status check_tc_solution(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solution& s)
 {
-    const int in = (s.kernel == TL_KERNEL_BF16X3) ? TL_DTYPE_BF16 : p.dtype_a;
+    const int in = is_split(s.kernel) ? TL_DTYPE_BF16 : p.dtype_a;
     if (in != TL_DTYPE_FP16 && in != TL_DTYPE_BF16 && in != TL_DTYPE_FP8_E4M3)
         return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel needs fp16, bf16 or fp8 operands");
     const int W = row_elems(in);
@@ -217,7 +220,7 @@ tl_status check_tc_solution(const tl_handle* h, const tl_gemm_problem& p, const 
     const int bm = s.macro_tile0;
     if (bm != 64 && bm != 128 && bm != 192 && bm != 256)
         return fail(TL_ERR_UNSUPPORTED, "macro_tile0 (m) must be 64, 128, 192 or 256");
-    const bool mmn = (s.kernel == TL_KERNEL_BF16X3) ? false : m_mn_major(p);
+    const bool mmn = m_mn_major(p);
     if (mmn && bm % W) return fail(TL_ERR_UNSUPPORTED, "macro_tile0 must be a multiple of the 128-byte row for MN-major A");
     if (s.depth_u != 0 && s.depth_u != W) return fail(TL_ERR_UNSUPPORTED, "depth_u is fixed to one 128-byte row");
     if (s.stages < 2 || s.stages > kTcMaxStages) return fail(TL_ERR_UNSUPPORTED, "stages must be in [2, 8]");
@@ -284,8 +287,9 @@ struct Prepared {
     const void* C;
     const void* A;
     const void* B;
-    // bf16x3 operand copies in the workspace
-    uint16_t *a_hi = nullptr, *a_lo = nullptr, *b_hi = nullptr, *b_lo = nullptr;
+    // split-precision operand pieces in the workspace (bf16x3: 2 per operand, bf16x6: 3)
+    uint16_t* a_pc[3] = {nullptr, nullptr, nullptr};
+    uint16_t* b_pc[3] = {nullptr, nullptr, nullptr};
     int64_t a_span = 0, b_span = 0;
     float* ws_partials = nullptr;
 };
@@ -348,24 +352,22 @@ tl_status prepare(tl_handle* h, const tl_gemm_problem* prob, const tl_gemm_solut
     }
     if (kernel == TL_KERNEL_TCGEN05 && p.dtype_a == TL_DTYPE_FP32)
         return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel needs fp16/bf16/fp8 inputs");
-    if (kernel == TL_KERNEL_BF16X3 && p.dtype_a != TL_DTYPE_FP32)
-        return fail(TL_ERR_UNSUPPORTED, "bf16x3 needs fp32 inputs");
+    if (is_split(kernel) && p.dtype_a != TL_DTYPE_FP32)
+        return fail(TL_ERR_UNSUPPORTED, "bf16x3/bf16x6 need fp32 inputs");
     if ((st = check_tc_solution(h, p, P.s)) != TL_SUCCESS) return st;
     if (p.m == 0 || p.n == 0 || p.k == 0) return TL_SUCCESS;
 
-    // workspace: [bf16x3 operands][split-k partials]
+    // workspace: [split pieces of A][split pieces of B][split-k partials]
     size_t need = 0;
-    size_t off_ahi = 0, off_alo = 0, off_bhi = 0, off_blo = 0, off_part = 0;
-    if (kernel == TL_KERNEL_BF16X3) {
+    size_t off_a[3] = {0, 0, 0}, off_b[3] = {0, 0, 0}, off_part = 0;
+    const int npc = split_pieces(kernel);
+    if (is_split(kernel)) {
         const int64_t a_rows = p.trans_a ? p.k : p.m, a_cols = p.trans_a ? p.m : p.k;
         const int64_t b_rows = p.trans_b ? p.n : p.k, b_cols = p.trans_b ? p.k : p.n;
         P.a_span = operand_span(p.lda, a_cols, p.batch, p.stride_a, a_rows);
         P.b_span = operand_span(p.ldb, b_cols, p.batch, p.stride_b, b_rows);
-        off_ahi = 0;
-        off_alo = align_up(off_ahi + P.a_span * 2, 256);
-        off_bhi = align_up(off_alo + P.a_span * 2, 256);
-        off_blo = align_up(off_bhi + P.b_span * 2, 256);
-        need = align_up(off_blo + P.b_span * 2, 256);
+        for (int i = 0; i < npc; ++i) { off_a[i] = need; need = align_up(need + P.a_span * 2, 256); }
+        for (int i = 0; i < npc; ++i) { off_b[i] = need; need = align_up(need + P.b_span * 2, 256); }
     }
     const int W = row_elems(tc_in_dtype(p));
     (void)W;
@@ -378,18 +380,18 @@ tl_status prepare(tl_handle* h, const tl_gemm_problem* prob, const tl_gemm_solut
     if (need) {
         if ((st = ensure_ws(h, need)) != TL_SUCCESS) return st;
         char* base = static_cast<char*>(h->ws);
-        if (kernel == TL_KERNEL_BF16X3) {
-            P.a_hi = reinterpret_cast<uint16_t*>(base + off_ahi);
-            P.a_lo = reinterpret_cast<uint16_t*>(base + off_alo);
-            P.b_hi = reinterpret_cast<uint16_t*>(base + off_bhi);
-            P.b_lo = reinterpret_cast<uint16_t*>(base + off_blo);
+        if (is_split(kernel)) {
+            for (int i = 0; i < npc; ++i) {
+                P.a_pc[i] = reinterpret_cast<uint16_t*>(base + off_a[i]);
+                P.b_pc[i] = reinterpret_cast<uint16_t*>(base + off_b[i]);
+            }
         }
         if (P.s.split_k > 1) P.ws_partials = reinterpret_cast<float*>(base + off_part);
     }
-    if (kernel == TL_KERNEL_BF16X3) {
+    if (is_split(kernel)) {
         // the split copies keep the caller's leading dimensions; TMA needs them 16-byte aligned in bf16
         if ((p.lda * 2) % 16 || (p.ldb * 2) % 16 || (p.batch > 1 && ((p.stride_a * 2) % 16 || (p.stride_b * 2) % 16)))
-            return fail(TL_ERR_UNSUPPORTED, "bf16x3: lda/ldb (and batch strides) must be multiples of 8 elements");
+            return fail(TL_ERR_UNSUPPORTED, "bf16x3/bf16x6: lda/ldb (and batch strides) must be multiples of 8 elements");
     }
     return TL_SUCCESS;
 }
@@ -419,25 +421,27 @@ tl_status enqueue(tl_handle* h, const Prepared& P, cudaStream_t s)
     L.in_dtype = tc_in_dtype(p);
     L.out_dtype = p.dtype_d;
     L.out_trunc = p.out_rounding;
-    L.x3 = (P.kernel == TL_KERNEL_BF16X3);
-    const void* A = P.A;
-    const void* B = P.B;
-    if (L.x3) {
+    L.pieces = split_pieces(P.kernel);
+    const void* Apc[3] = {P.A, nullptr, nullptr};
+    const void* Bpc[3] = {P.B, nullptr, nullptr};
+    if (L.pieces > 1) {
         const int64_t a_rows = p.trans_a ? p.k : p.m, a_cols = p.trans_a ? p.m : p.k;
         const int64_t b_rows = p.trans_b ? p.n : p.k, b_cols = p.trans_b ? p.k : p.n;
-        tl_status st = aux_split_bf16x2(static_cast<const float*>(P.A), a_rows, a_cols, p.lda, p.batch, p.stride_a,
-                                        P.a_hi, P.a_lo, s, &h->launches);
+        tl_status st = aux_split_bf16(static_cast<const float*>(P.A), a_rows, a_cols, p.lda, p.batch, p.stride_a,
+                                      P.a_pc[0], P.a_pc[1], P.a_pc[2], s, &h->launches);
         if (st != TL_SUCCESS) return st;
-        st = aux_split_bf16x2(static_cast<const float*>(P.B), b_rows, b_cols, p.ldb, p.batch, p.stride_b, P.b_hi,
-                              P.b_lo, s, &h->launches);
+        st = aux_split_bf16(static_cast<const float*>(P.B), b_rows, b_cols, p.ldb, p.batch, p.stride_b, P.b_pc[0],
+                            P.b_pc[1], P.b_pc[2], s, &h->launches);
         if (st != TL_SUCCESS) return st;
-        A = P.a_hi;
-        B = P.b_hi;
-        L.opM_lo = {P.a_lo, p.m, p.lda, p.stride_a, m_mn_major(p) ? 1 : 0};
-        L.opN_lo = {P.b_lo, p.n, p.ldb, p.stride_b, n_mn_major(p) ? 1 : 0};
+        for (int i = 0; i < L.pieces; ++i) {
+            Apc[i] = P.a_pc[i];
+            Bpc[i] = P.b_pc[i];
+        }
     }
-    L.opM = {A, p.m, p.lda, p.stride_a, m_mn_major(p) ? 1 : 0};
-    L.opN = {B, p.n, p.ldb, p.stride_b, n_mn_major(p) ? 1 : 0};
+    for (int i = 0; i < L.pieces; ++i) {
+        L.opM[i] = {Apc[i], p.m, p.lda, p.stride_a, m_mn_major(p) ? 1 : 0};
+        L.opN[i] = {Bpc[i], p.n, p.ldb, p.stride_b, n_mn_major(p) ? 1 : 0};
+    }
     L.M = p.m; L.N = p.n; L.K = p.k; L.batch = p.batch;
     L.D = P.D; L.C = (p.beta != 0.0f) ? P.C : nullptr;
     L.ldd = p.ldd; L.ldc = p.ldc; L.stride_d = p.stride_d; L.stride_c = p.stride_c;
@@ -459,7 +463,7 @@ tl_status enqueue(tl_handle* h, const Prepared& P, cudaStream_t s)
 std::vector<tl_gemm_solution> tc_candidates(const tl_handle* h, const tl_gemm_problem& p, int kernel)
 {
     std::vector<std::pair<double, tl_gemm_solution>> ranked;
-    const int in = (kernel == TL_KERNEL_BF16X3) ? TL_DTYPE_BF16 : p.dtype_a;
+    const int in = is_split(kernel) ? TL_DTYPE_BF16 : p.dtype_a;
     const int W = row_elems(in);
     const int64_t num_kb = std::max<int64_t>(1, (p.k + W - 1) / W);
     const int64_t tiles_n = (p.n + kTcTileN - 1) / kTcTileN;
@@ -654,10 +658,10 @@ TL_API tl_status tl_check_solution(tl_handle* h, const tl_gemm_problem* p, const
             return fail(TL_ERR_UNSUPPORTED, "SIMT kernel supports macro tile 128x128, depth_u 8, split_k 1");
         return TL_SUCCESS;
     }
-    if (s->kernel != TL_KERNEL_TCGEN05 && s->kernel != TL_KERNEL_BF16X3)
-        return fail(TL_ERR_INVALID_ARG, "solution kernel must be resolved (SIMT, TCGEN05 or BF16X3)");
-    if (s->kernel == TL_KERNEL_BF16X3 && p->dtype_a != TL_DTYPE_FP32)
-        return fail(TL_ERR_UNSUPPORTED, "bf16x3 needs fp32 inputs");
+    if (s->kernel != TL_KERNEL_TCGEN05 && !is_split(s->kernel))
+        return fail(TL_ERR_INVALID_ARG, "solution kernel must be resolved (SIMT, TCGEN05, BF16X3 or BF16X6)");
+    if (is_split(s->kernel) && p->dtype_a != TL_DTYPE_FP32)
+        return fail(TL_ERR_UNSUPPORTED, "bf16x3/bf16x6 need fp32 inputs");
     if (s->kernel == TL_KERNEL_TCGEN05 && p->dtype_a == TL_DTYPE_FP32)
         return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel needs fp16/bf16/fp8 inputs");
     return check_tc_solution(h, *p, *s);
@@ -1039,8 +1043,8 @@ TL_API tl_status tl_quantize_fp8(tl_handle* h, tl_dtype src_dtype, const void* s
 TL_API tl_status tl_split_bf16x2(tl_handle* h, const float* src, int64_t n, void* hi, void* lo, void* stream)
 {
     if (!h || n < 0 || (n && (!src || !hi || !lo))) return fail(TL_ERR_INVALID_ARG, "bad argument");
-    return aux_split_bf16x2(src, n, 1, n, 1, n, static_cast<uint16_t*>(hi), static_cast<uint16_t*>(lo), S(stream),
-                            &h->launches);
+    return aux_split_bf16(src, n, 1, n, 1, n, static_cast<uint16_t*>(hi), static_cast<uint16_t*>(lo), nullptr,
+                          S(stream), &h->launches);
 }
 
 // ---- verification ------------------------------------------------------------------------------------

@@ -64,12 +64,11 @@ struct TcGroupEntry {   // aligned like CUtensorMap
 
 struct TcLaunch {
     // operands
-    int in_dtype;            // FP16 / BF16 / FP8_E4M3 (BF16 for the bf16x3 path)
+    int in_dtype;            // FP16 / BF16 / FP8_E4M3 (BF16 for the fp32 split paths)
     int out_dtype;
     int out_trunc;
-    TcOperand opN, opM;      // hi parts
-    TcOperand opN_lo, opM_lo;  // bf16x3 lo parts (ptr == nullptr otherwise)
-    int x3;                  // bf16x3 mode
+    TcOperand opN[3], opM[3];  // operand pieces: [0] the operand (or its bf16 head), [1..2] residuals
+    int pieces;              // 1 plain, 2 = bf16x3 (3 products), 3 = bf16x6 (6 products)
     int64_t M, N, K, batch;
     void* D;
     const void* C;
@@ -122,8 +121,10 @@ struct SimtLaunch {
 tl_status simt_gemm_launch(const SimtLaunch& L, cudaStream_t stream, int64_t* launches);
 
 // ---- auxiliary kernels ------------------------------------------------------------------------------
-tl_status aux_split_bf16x2(const float* src, int64_t rows, int64_t cols, int64_t ld, int64_t batch,
-                           int64_t batch_stride, uint16_t* hi, uint16_t* lo, cudaStream_t s, int64_t* launches);
+// x = p0 + p1 (+ p2): each piece the bf16 rounding (RNE) of what the previous pieces leave; p2 may be null.
+tl_status aux_split_bf16(const float* src, int64_t rows, int64_t cols, int64_t ld, int64_t batch,
+                         int64_t batch_stride, uint16_t* p0, uint16_t* p1, uint16_t* p2, cudaStream_t s,
+                         int64_t* launches);
 tl_status aux_amax(int src_dtype, const void* src, int64_t n, float* amax_dev, cudaStream_t s, int64_t* launches);
 tl_status aux_quant_e4m3(int src_dtype, const void* src, int64_t n, const float* amax_dev, uint8_t* dst,
                          float* scale_out_dev, cudaStream_t s, int64_t* launches);

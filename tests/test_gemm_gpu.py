@@ -183,25 +183,46 @@ def test_unaligned_ld_falls_back_to_simt(h):
 
 
 # ---------------------------------------------------------------------------- bf16x3 and fp8
-def test_bf16x3_accuracy_beats_fp32_simt(h):
+def _fp32_paths_errors(h, M, N, K, cols):
+    """Errors of the three fp32 paths against FP64 on `cols` output columns of an M x N x K NN GEMM
+    with A, B uniform[-1,1) (seed 2)."""
     import torch
     g = orc.rng(2)
-    M = N = K = 1024
     A = orc.uniform_pm1(g, M * K).astype(np.float32)
     B = orc.uniform_pm1(g, K * N).astype(np.float32)
     dA, dB = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
-    ref, absprod = orc.gemm_f64_numpy(False, False, M, N, K, 1.0, A, M, B, K)
+    sel = np.sort(np.random.default_rng(0).choice(N, cols, replace=False))
+    opA = A.reshape(K, M).T.astype(np.float64)
+    opB = B.reshape(N, K)[sel].T.astype(np.float64)
+    ref = opA @ opB
+    absprod = np.abs(opA) @ np.abs(opB)
     errs = {}
-    for kern in ("bf16x3", "simt"):
+    for kern in ("bf16x6", "bf16x3", "simt"):
         D = torch.empty(M * N, dtype=torch.float32, device="cuda")
         h.gemm(tl.Problem.make(M, N, K, dtype="fp32", kernel=kern), D, None, dA, dB)
-        got = gu.mat(D.cpu().numpy(), M, N, M)
-        errs[kern] = orc.normwise_error(got, ref)
-        assert orc.componentwise_error(got, ref, absprod) < 1e-6
-    assert errs["bf16x3"] < 2e-6, errs
+        got = D.cpu().numpy().reshape(N, M)[sel].T
+        errs[kern] = (orc.normwise_error(got, ref), orc.componentwise_error(got, ref, absprod))
+    return errs
 
 
-def test_split_bf16x2_exact(h):
+def test_fp32_accurate_paths_1024(h):
+    errs = _fp32_paths_errors(h, 1024, 1024, 1024, 256)
+    print("fp32 paths 1024^3 (normwise, componentwise):", errs)
+    assert errs["bf16x6"][0] < 1e-6
+    assert errs["bf16x3"][0] < 4e-6          # two-piece split: products good to ~2^-17
+    assert errs["simt"][0] < 4e-6
+    assert all(e[1] < 1e-6 for e in errs.values())
+
+
+def test_fp32_accurate_paths_8192(h):
+    """The FP32-accurate configuration: 8192^3 NN, checked on 128 output columns against FP64."""
+    errs = _fp32_paths_errors(h, 8192, 8192, 8192, 128)
+    print("fp32 paths 8192^3 (normwise, componentwise):", errs)
+    assert errs["bf16x6"][0] <= 1e-6
+    assert errs["bf16x6"][0] < errs["simt"][0]
+
+
+def test_split_bf16_pieces_exact(h):
     import torch
     g = np.random.default_rng(8)
     x = (g.standard_normal(10001) * 10).astype(np.float32)
