@@ -104,7 +104,10 @@ typedef struct tl_gemm_problem {
  * TCGEN05: macro_tile1 is the tcgen05 M extent (128, problem n maps to TMEM lanes) and
  * macro_tile0 is the tcgen05 N extent (64, 128, 192 or 256 along m); depth_u is fixed by the
  * input type (64 for 16-bit, 128 for fp8: one 128-byte swizzle row).  split_k > 1 divides k
- * across CTAs and reduces through a device workspace owned by the handle. */
+ * across CTAs and reduces through a device workspace owned by the handle.
+ * promote_k > 0 (TCGEN05/BF16X3/BF16X6 with macro_tile0 == 128): the dominant product restarts its
+ * tensor-core accumulation every promote_k elements of k and the chains are summed in fp32 on the
+ * CUDA cores (tensor-core accumulation error grows with the chain length). */
 typedef struct tl_gemm_solution {
     int32_t kernel;            /* resolved tl_kernel (never AUTO once filled in) */
     int32_t macro_tile0;
@@ -116,7 +119,8 @@ typedef struct tl_gemm_solution {
     int32_t split_k;           /* >= 1 */
     int32_t raster;            /* tile rasterisation group width in tiles (0 = linear order) */
     int32_t ctas;              /* persistent CTAs (0 = one per SM) */
-    int32_t reserved[6];
+    int32_t promote_k;         /* k per tensor-core accumulation chain (0 = the whole k range) */
+    int32_t reserved[5];
 } tl_gemm_solution;
 
 /* ---- handles and errors --------------------------------------------------------------------- */

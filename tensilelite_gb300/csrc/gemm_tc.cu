@@ -50,7 +50,9 @@ struct TcKernelParams {
     float alpha, beta;
     int bm, stages, split_k, raster;
     int nterms;                   // tensor-core products per k-block (1, or 3 / 6 for the fp32 split)
-    uint8_t term_n[8], term_m[8]; // piece of B / of A used by each product
+    uint8_t term_n[8], term_m[8]; // piece of B / of A used by each product (the last is A0*B0)
+    int promote_kb;               // >0: the A0*B0 product restarts its TMEM chain every promote_kb
+                                  // k-blocks; the epilogue adds each chain into fp32 registers
     int tiles_m, tiles_n;
     int64_t total_work;
     int num_kb;
@@ -269,6 +271,52 @@ __device__ __forceinline__ void store_chunk(const TileJob& j, int64_t base_c, in
     }
 }
 
+// Split-k completion, run by the four epilogue warps after this split parked its partial tile in
+// the workspace: the last split of a tile to arrive (per-tile counter) sums every split's partial
+// in split order -- so the result does not depend on which CTA finished last -- and runs the
+// epilogue.  The counter is reset for the next launch.  Every thread passes the same three named
+// barriers whether or not it has work, so a warp that gave up on a wait cannot strand the others.
+template <typename TD>
+__device__ __forceinline__ void split_finish(const TcKernelParams& p, const TileJob& j, bool ok, int et, int row,
+                                             bool row_ok, int64_t base_c, int64_t base_d, volatile int* last_flag)
+{
+    __threadfence();
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    if (et == 0) {
+        int last = 0;
+        if (ok) last = (atomicAdd(p.counters + j.tile, 1) == p.split_k - 1) ? 1 : 0;
+        *last_flag = last;
+    }
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    const int is_last = *last_flag;
+    if (is_last && ok) {
+        __threadfence();
+        const int chunks = p.bm / 32;
+        for (int c = 0; c < chunks; ++c) {
+            float v[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) v[i] = 0.f;
+            for (int s = 0; s < p.split_k; ++s) {
+                const float4* src = reinterpret_cast<const float4*>(
+                    p.ws + (static_cast<size_t>(j.tile) * p.split_k + s) * (static_cast<size_t>(kTcTileN) * p.bm) +
+                    (static_cast<size_t>(c) * kTcTileN + row) * 32);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const float4 f = __ldcg(src + q);
+                    v[4 * q] += f.x;
+                    v[4 * q + 1] += f.y;
+                    v[4 * q + 2] += f.z;
+                    v[4 * q + 3] += f.w;
+                }
+            }
+            const int m = j.m0 + c * 32;
+            if (row_ok && m < j.M) store_chunk<TD>(j, base_c, base_d, m, v, p.out_trunc);
+        }
+        if (et == 0) p.counters[j.tile] = 0;   // ready for the next launch
+    }
+    asm volatile("bar.sync 1, 128;" ::: "memory");   // last_flag is reused by the next tile
+}
+
 template <int KIND, typename TD>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_constant__ TcKernelParams p)
 {
@@ -278,15 +326,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
     const uint32_t stage_bytes = tileN_bytes + static_cast<uint32_t>(p.bm) * kTcRowBytes;
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(p.stages) * stage_bytes);
     uint64_t* empty = full + kTcMaxStages;
-    uint64_t* tfull = empty + kTcMaxStages;
+    uint64_t* tfull = empty + kTcMaxStages;     // main accumulator buffers (per tile, or per chain)
     uint64_t* tempty = tfull + 2;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tempty + 2);
+    uint64_t* sfull = tempty + 2;               // small-term accumulators (promotion with split terms)
+    uint64_t* sempty = sfull + 2;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sempty + 2);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     volatile int* last_flag = abort_flag + 1;
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const uint32_t tmem_cols = (2 * p.bm <= 128) ? 128u : (2 * p.bm <= 256 ? 256u : 512u);
+    const bool promo = p.promote_kb > 0;
+    const bool sep_small = promo && p.nterms > 1;
+    // TMEM columns: main accumulator x2 (+ small-term accumulator x2 when they are kept apart)
+    const uint32_t need_cols = static_cast<uint32_t>(p.bm) * (sep_small ? 4u : 2u);
+    const uint32_t tmem_cols = need_cols <= 128 ? 128u : (need_cols <= 256 ? 256u : 512u);
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < p.stages; ++s) {
@@ -296,6 +350,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
         for (int a = 0; a < 2; ++a) {
             ptx::mbar_init(&tfull[a], 1);
             ptx::mbar_init(&tempty[a], 128);
+            ptx::mbar_init(&sfull[a], 1);
+            ptx::mbar_init(&sempty[a], 128);
         }
         *abort_flag = 0;
         *last_flag = 0;
@@ -364,46 +420,78 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
         }
     } else if (warp == 1) {
         // ------------------------------------------------------------------ MMA issuer
+        // Without promotion a tile's whole k range accumulates in one TMEM buffer (two buffers
+        // alternate between tiles).  With promotion the A0*B0 product restarts its accumulation
+        // every promote_kb k-blocks in the alternate buffer (the epilogue drains each chain into
+        // fp32 registers), and the small split-precision products accumulate for the whole tile in
+        // a separate pair of buffers.
         if (lane == 0) {
-            uint32_t stage = 0, phase = 0, acc = 0, acc_phase = 0;
+            uint32_t stage = 0, phase = 0, mbuf = 0, mph = 0, sbuf = 0, sph = 0;
             bool ok = true;
             for (int64_t w = blockIdx.x; w < p.total_work && ok; w += gridDim.x) {
                 TileJob j;
                 get_job(p, w, j);
-                if (!ptx::mbar_wait(&tempty[acc], acc_phase ^ 1u, tlim, abort_flag)) {
-                    record_error(p, abort_flag, 2);
-                    break;
+                const int nkb = j.kb1 - j.kb0;
+                const int chunk = promo ? p.promote_kb : (nkb > 0 ? nkb : 1);
+                if (sep_small) {
+                    if (!ptx::mbar_wait(&sempty[sbuf], sph ^ 1u, tlim, abort_flag)) {
+                        record_error(p, abort_flag, 2);
+                        break;
+                    }
+                    ptx::tc_fence_after();
                 }
-                ptx::tc_fence_after();
-                const uint32_t d_tmem = tmem_base + acc * static_cast<uint32_t>(p.bm);
-                const int nblk = (j.kb1 - j.kb0) * nvirt;
-                for (int i = 0; i < nblk; ++i) {
-                    if (!ptx::mbar_wait(&full[stage], phase, tlim, abort_flag)) {
-                        record_error(p, abort_flag, 4);
+                bool small_started = false;
+                for (int c0 = 0; c0 < nkb && ok; c0 += chunk) {
+                    if (!ptx::mbar_wait(&tempty[mbuf], mph ^ 1u, tlim, abort_flag)) {
+                        record_error(p, abort_flag, 2);
                         ok = false;
                         break;
                     }
                     ptx::tc_fence_after();
-                    const uint32_t sN = ptx::smem_u32(smem + static_cast<size_t>(stage) * stage_bytes);
-                    const uint32_t sM = sN + tileN_bytes;
+                    bool main_started = false;
+                    const int c1 = (c0 + chunk < nkb) ? c0 + chunk : nkb;
+                    for (int kb = c0; kb < c1 && ok; ++kb) {
+                        for (int v = 0; v < nvirt; ++v) {
+                            if (!ptx::mbar_wait(&full[stage], phase, tlim, abort_flag)) {
+                                record_error(p, abort_flag, 4);
+                                ok = false;
+                                break;
+                            }
+                            ptx::tc_fence_after();
+                            const bool is_main = !sep_small || v == nvirt - 1;
+                            const uint32_t d_tmem = tmem_base + (is_main ? mbuf * static_cast<uint32_t>(p.bm)
+                                                                         : (2u + sbuf) * static_cast<uint32_t>(p.bm));
+                            const bool started = is_main ? main_started : small_started;
+                            const uint32_t sN = ptx::smem_u32(smem + static_cast<size_t>(stage) * stage_bytes);
+                            const uint32_t sM = sN + tileN_bytes;
 #pragma unroll
-                    for (int ks = 0; ks < 4; ++ks) {
-                        const uint64_t adesc = ptx::sdesc_sw128(sN + ks * p.n_kstep, p.n_lbo, 1024);
-                        const uint64_t bdesc = ptx::sdesc_sw128(sM + ks * p.m_kstep, p.m_lbo, 1024);
-                        const uint32_t accumulate = (i > 0 || ks > 0) ? 1u : 0u;
-                        if (KIND == 0) ptx::mma_f16(d_tmem, adesc, bdesc, p.idesc, accumulate);
-                        else ptx::mma_f8(d_tmem, adesc, bdesc, p.idesc, accumulate);
+                            for (int ks = 0; ks < 4; ++ks) {
+                                const uint64_t adesc = ptx::sdesc_sw128(sN + ks * p.n_kstep, p.n_lbo, 1024);
+                                const uint64_t bdesc = ptx::sdesc_sw128(sM + ks * p.m_kstep, p.m_lbo, 1024);
+                                const uint32_t accumulate = (started || ks > 0) ? 1u : 0u;
+                                if (KIND == 0) ptx::mma_f16(d_tmem, adesc, bdesc, p.idesc, accumulate);
+                                else ptx::mma_f8(d_tmem, adesc, bdesc, p.idesc, accumulate);
+                            }
+                            if (is_main) main_started = true;
+                            else small_started = true;
+                            ptx::mma_commit(&empty[stage]);
+                            if (++stage == static_cast<uint32_t>(p.stages)) {
+                                stage = 0;
+                                phase ^= 1u;
+                            }
+                        }
                     }
-                    ptx::mma_commit(&empty[stage]);
-                    if (++stage == static_cast<uint32_t>(p.stages)) {
-                        stage = 0;
-                        phase ^= 1u;
-                    }
+                    if (!ok) break;
+                    ptx::mma_commit(&tfull[mbuf]);
+                    mbuf ^= 1u;
+                    if (mbuf == 0) mph ^= 1u;
                 }
                 if (!ok) break;
-                ptx::mma_commit(&tfull[acc]);
-                acc ^= 1u;
-                if (acc == 0) acc_phase ^= 1u;
+                if (sep_small) {
+                    ptx::mma_commit(&sfull[sbuf]);
+                    sbuf ^= 1u;
+                    if (sbuf == 0) sph ^= 1u;
+                }
             }
         }
     } else {
@@ -414,23 +502,108 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
         const int quarter = warp & 3;             // TMEM lanes 32*quarter .. +31
         const int row = quarter * 32 + lane;      // tile row = problem n offset
         const int et = threadIdx.x - 64;          // 0..127
-        uint32_t acc = 0, acc_phase = 0;
+        const uint32_t lane_off = static_cast<uint32_t>(quarter * 32) << 16;
+        uint32_t mbuf = 0, mph = 0, sbuf = 0, sph = 0;
         const int chunks = p.bm / 32;
         bool ok = true;
         for (int64_t w = blockIdx.x; w < p.total_work; w += gridDim.x) {
             TileJob j;
             get_job(p, w, j);
-            bool got = ok && ptx::mbar_wait(&tfull[acc], acc_phase, tlim, abort_flag);
+            const int n = j.n0 + row;
+            const bool row_ok = n < j.N;
+            const int64_t base_d = static_cast<int64_t>(j.b) * p.stride_d + static_cast<int64_t>(n) * j.ldd;
+            const int64_t base_c = static_cast<int64_t>(j.b) * p.stride_c + static_cast<int64_t>(n) * j.ldc;
+            if (promo) {
+                // ---- promotion: sum the A0*B0 chains (and the small terms) in fp32 registers; bm == 128
+                float run[128];
+#pragma unroll
+                for (int i = 0; i < 128; ++i) run[i] = 0.f;
+                const int nkb = j.kb1 - j.kb0;
+                const int nchain = (nkb + p.promote_kb - 1) / p.promote_kb;
+                for (int c = 0; c < nchain; ++c) {
+                    bool got = ok && ptx::mbar_wait(&tfull[mbuf], mph, tlim, abort_flag);
+                    got = __all_sync(0xffffffffu, got);
+                    if (ok && !got) {
+                        if (lane == 0) record_error(p, abort_flag, 8);
+                        ok = false;
+                    }
+                    if (ok) {
+                        ptx::tc_fence_after();
+                        const uint32_t tb = tmem_base + lane_off + mbuf * static_cast<uint32_t>(p.bm);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            uint32_t r[32];
+                            __syncwarp();
+                            ptx::tmem_ld32(tb + q * 32, r);
+#pragma unroll
+                            for (int i = 0; i < 32; ++i) run[q * 32 + i] += __uint_as_float(r[i]);
+                        }
+                        ptx::tc_fence_before();
+                        ptx::mbar_arrive(&tempty[mbuf]);
+                    }
+                    mbuf ^= 1u;
+                    if (mbuf == 0) mph ^= 1u;
+                }
+                if (sep_small) {
+                    bool got = ok && ptx::mbar_wait(&sfull[sbuf], sph, tlim, abort_flag);
+                    got = __all_sync(0xffffffffu, got);
+                    if (ok && !got) {
+                        if (lane == 0) record_error(p, abort_flag, 8);
+                        ok = false;
+                    }
+                    if (ok) {
+                        ptx::tc_fence_after();
+                        const uint32_t tb = tmem_base + lane_off + (2u + sbuf) * static_cast<uint32_t>(p.bm);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            uint32_t r[32];
+                            __syncwarp();
+                            ptx::tmem_ld32(tb + q * 32, r);
+#pragma unroll
+                            for (int i = 0; i < 32; ++i) run[q * 32 + i] += __uint_as_float(r[i]);
+                        }
+                        ptx::tc_fence_before();
+                        ptx::mbar_arrive(&sempty[sbuf]);
+                    }
+                    sbuf ^= 1u;
+                    if (sbuf == 0) sph ^= 1u;
+                }
+                if (p.split_k == 1) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int m = j.m0 + q * 32;
+                        if (ok && row_ok && m < j.M) {
+                            float v[32];
+#pragma unroll
+                            for (int i = 0; i < 32; ++i) v[i] = run[q * 32 + i];
+                            store_chunk<TD>(j, base_c, base_d, m, v, p.out_trunc);
+                        }
+                    }
+                } else {
+                    float* slab = p.ws + (static_cast<size_t>(j.tile) * p.split_k + j.split) *
+                                             (static_cast<size_t>(kTcTileN) * p.bm);
+                    if (ok) {
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            float4* dst = reinterpret_cast<float4*>(slab + (static_cast<size_t>(q) * kTcTileN + row) * 32);
+#pragma unroll
+                            for (int e = 0; e < 8; ++e)
+                                __stcg(dst + e, make_float4(run[q * 32 + 4 * e], run[q * 32 + 4 * e + 1],
+                                                            run[q * 32 + 4 * e + 2], run[q * 32 + 4 * e + 3]));
+                        }
+                    }
+                    split_finish<TD>(p, j, ok, et, row, row_ok, base_c, base_d, last_flag);
+                }
+                continue;
+            }
+            // ---- one TMEM accumulator per tile
+            bool got = ok && ptx::mbar_wait(&tfull[mbuf], mph, tlim, abort_flag);
             got = __all_sync(0xffffffffu, got);
             if (ok && !got) {
                 if (lane == 0) record_error(p, abort_flag, 8);
                 ok = false;
             }
-            const int n = j.n0 + row;
-            const bool row_ok = n < j.N;
-            const int64_t base_d = static_cast<int64_t>(j.b) * p.stride_d + static_cast<int64_t>(n) * j.ldd;
-            const int64_t base_c = static_cast<int64_t>(j.b) * p.stride_c + static_cast<int64_t>(n) * j.ldc;
-            const uint32_t tbase = tmem_base + (static_cast<uint32_t>(quarter * 32) << 16) + acc * p.bm;
+            const uint32_t tbase = tmem_base + lane_off + mbuf * static_cast<uint32_t>(p.bm);
             if (ok) ptx::tc_fence_after();
             if (p.split_k == 1) {
                 for (int c = 0; c < chunks && ok; ++c) {
@@ -439,7 +612,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                     ptx::tmem_ld32(tbase + c * 32, r);
                     if (c == chunks - 1) {
                         ptx::tc_fence_before();
-                        ptx::mbar_arrive(&tempty[acc]);
+                        ptx::mbar_arrive(&tempty[mbuf]);
                     }
                     const int m = j.m0 + c * 32;
                     if (row_ok && m < j.M) {
@@ -459,7 +632,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                     ptx::tmem_ld32(tbase + c * 32, r);
                     if (c == chunks - 1) {
                         ptx::tc_fence_before();
-                        ptx::mbar_arrive(&tempty[acc]);
+                        ptx::mbar_arrive(&tempty[mbuf]);
                     }
                     float4* dst = reinterpret_cast<float4*>(slab + (static_cast<size_t>(c) * kTcTileN + row) * 32);
 #pragma unroll
@@ -467,43 +640,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         __stcg(dst + q, make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
                                                     __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3])));
                 }
-                __threadfence();
-                asm volatile("bar.sync 1, 128;" ::: "memory");
-                if (et == 0) {
-                    int last = 0;
-                    if (ok) last = (atomicAdd(p.counters + j.tile, 1) == p.split_k - 1) ? 1 : 0;
-                    *last_flag = last;
-                }
-                asm volatile("bar.sync 1, 128;" ::: "memory");
-                const int is_last = *last_flag;
-                if (is_last && ok) {
-                    __threadfence();
-                    for (int c = 0; c < chunks; ++c) {
-                        float v[32];
-#pragma unroll
-                        for (int i = 0; i < 32; ++i) v[i] = 0.f;
-                        for (int s = 0; s < p.split_k; ++s) {
-                            const float4* src = reinterpret_cast<const float4*>(
-                                p.ws + (static_cast<size_t>(j.tile) * p.split_k + s) * (static_cast<size_t>(kTcTileN) * p.bm) +
-                                (static_cast<size_t>(c) * kTcTileN + row) * 32);
-#pragma unroll
-                            for (int q = 0; q < 8; ++q) {
-                                const float4 f = __ldcg(src + q);
-                                v[4 * q] += f.x;
-                                v[4 * q + 1] += f.y;
-                                v[4 * q + 2] += f.z;
-                                v[4 * q + 3] += f.w;
-                            }
-                        }
-                        const int m = j.m0 + c * 32;
-                        if (row_ok && m < j.M) store_chunk<TD>(j, base_c, base_d, m, v, p.out_trunc);
-                    }
-                    if (et == 0) p.counters[j.tile] = 0;   // ready for the next launch
-                }
-                asm volatile("bar.sync 1, 128;" ::: "memory");   // last_flag is reused next tile
+                split_finish<TD>(p, j, ok, et, row, row_ok, base_c, base_d, last_flag);
             }
-            acc ^= 1u;
-            if (acc == 0) acc_phase ^= 1u;
+            mbuf ^= 1u;
+            if (mbuf == 0) mph ^= 1u;
         }
     }
 
@@ -688,6 +828,7 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     kp.tiles_n = static_cast<int>((L.N + kTcTileN - 1) / kTcTileN);
     kp.num_kb = static_cast<int>((L.K + W - 1) / W);
     kp.kb_elems = W;
+    kp.promote_kb = L.promote_k > 0 ? static_cast<int>((L.promote_k + W - 1) / W) : 0;
     kp.total_work = static_cast<int64_t>(kp.tiles_m) * kp.tiles_n * L.batch * L.split_k;
     kp.n_mn_major = L.opN[0].mn_major;
     kp.m_mn_major = L.opM[0].mn_major;

@@ -199,6 +199,17 @@ void tc_heuristic(const tl_handle* h, const tl_gemm_problem& p, int kernel, tl_g
         split = static_cast<int>(std::min<int64_t>(h->sm_count / std::max<int64_t>(1, tiles), num_kb / 4));
         split = std::max(1, std::min(split, 16));
     }
+    if (is_split(kernel)) {
+        // FP32-accurate paths: 128-wide tiles so the dominant product can be promoted out of TMEM
+        // every 256 k (the chain length sets the tensor-core accumulation error)
+        bm = 128;
+        s->promote_k = 256;
+        const int64_t t128 = tiles_n * ((p.m + 127) / 128) * p.batch;
+        split = 1;
+        if (t128 < h->sm_count / 2 && num_kb >= 8)
+            split = std::max(1, static_cast<int>(std::min<int64_t>(std::min<int64_t>(h->sm_count / std::max<int64_t>(1, t128),
+                                                                                     num_kb / 4), 16)));
+    }
     s->macro_tile0 = bm;
     s->macro_tile1 = kTcTileN;
     s->depth_u = W;
@@ -229,6 +240,9 @@ tl_status check_tc_solution(const tl_handle* h, const tl_gemm_problem& p, const 
     if (s.split_k < 1 || (num_kb > 0 && s.split_k > num_kb) || s.split_k > 64)
         return fail(TL_ERR_UNSUPPORTED, "split_k must be in [1, min(64, k blocks)]");
     if (s.raster < 0 || s.ctas < 0) return fail(TL_ERR_INVALID_ARG, "raster and ctas must be >= 0");
+    if (s.promote_k < 0) return fail(TL_ERR_INVALID_ARG, "promote_k must be >= 0");
+    if (s.promote_k > 0 && bm != 128)
+        return fail(TL_ERR_UNSUPPORTED, "promote_k needs macro_tile0 == 128 (fp32 running sums, TMEM budget)");
     return TL_SUCCESS;
 }
 
@@ -277,6 +291,23 @@ tl_status ensure_counters(tl_handle* h, size_t n)
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// The driver-API calls (tensor-map encoding) need the device's primary context current on the calling
+// thread; a thread that has only made runtime calls so far (e.g. an autograd worker) may not have it.
+// cudaSetDevice on the already-current device binds it.  Once per thread and device.
+tl_status bind_thread(const tl_handle* h)
+{
+    static thread_local int bound = -1;
+    if (bound == h->device) return TL_SUCCESS;
+    int cur = -1;
+    TL_CUDA_TRY(cudaGetDevice(&cur));
+    if (cur != h->device)
+        return fail(TL_ERR_INVALID_ARG, "handle belongs to device " + std::to_string(h->device) +
+                                            " but the current device is " + std::to_string(cur));
+    TL_CUDA_TRY(cudaSetDevice(cur));
+    bound = cur;
+    return TL_SUCCESS;
+}
+
 // Everything a GEMM launch needs once the solution is fixed; preparing allocates, enqueueing
 // only launches (so enqueue can be captured in a CUDA graph).
 struct Prepared {
@@ -303,7 +334,9 @@ int64_t operand_span(int64_t ld, int64_t cols, int64_t batch, int64_t bstride, i
 tl_status prepare(tl_handle* h, const tl_gemm_problem* prob, const tl_gemm_solution* sol, void* D, const void* C,
                   const void* A, const void* B, Prepared* out)
 {
-    tl_status st = validate(prob);
+    tl_status st = bind_thread(h);
+    if (st != TL_SUCCESS) return st;
+    st = validate(prob);
     if (st != TL_SUCCESS) return st;
     Prepared& P = *out;
     P.p = *prob;
@@ -451,6 +484,7 @@ tl_status enqueue(tl_handle* h, const Prepared& P, cudaStream_t s)
     L.split_k = P.s.split_k;
     L.raster = P.s.raster;
     L.ctas = P.s.ctas;
+    L.promote_k = P.s.promote_k;
     L.err = h->d_err;
     L.timeout_ns = h->timeout_ns;
     L.workspace = P.ws_partials;
@@ -480,6 +514,7 @@ std::vector<tl_gemm_solution> tc_candidates(const tl_handle* h, const tl_gemm_pr
                 s.stages = max_stages(bm, h->smem_optin);
                 s.split_k = split;
                 s.raster = raster;
+                if (is_split(kernel)) s.promote_k = 256;
                 if (raster && raster >= tiles_n) continue;
                 if (check_tc_solution(h, p, s) != TL_SUCCESS) continue;
                 // cost model: tensor work per tile grows with bm (efficiency of the 128 x bm MMA),
@@ -503,7 +538,8 @@ std::vector<tl_gemm_solution> tc_candidates(const tl_handle* h, const tl_gemm_pr
 
 tl_status save_cache(const char* path, const std::string& key, const tl_gemm_solution& s, float ms)
 {
-    // line-oriented JSON object: "key": [kernel, mt0, mt1, du, stages, wt0, wt1, split, raster, ctas, ms]
+    // line-oriented JSON object:
+    //   "key": [kernel, mt0, mt1, du, stages, wt0, wt1, split, raster, ctas, promote_k, ms]
     std::map<std::string, std::string> lines;
     {
         std::ifstream in(path);
@@ -519,8 +555,9 @@ tl_status save_cache(const char* path, const std::string& key, const tl_gemm_sol
         }
     }
     char buf[256];
-    snprintf(buf, sizeof(buf), " [%d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %.6f]", s.kernel, s.macro_tile0,
-             s.macro_tile1, s.depth_u, s.stages, s.wave_tile0, s.wave_tile1, s.split_k, s.raster, s.ctas, ms);
+    snprintf(buf, sizeof(buf), " [%d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %.6f]", s.kernel, s.macro_tile0,
+             s.macro_tile1, s.depth_u, s.stages, s.wave_tile0, s.wave_tile1, s.split_k, s.raster, s.ctas,
+             s.promote_k, ms);
     lines[key] = buf;
     std::ofstream out(path, std::ios::trunc);
     if (!out) return fail(TL_ERR_INVALID_ARG, std::string("cannot write ") + path);
@@ -754,9 +791,9 @@ TL_API tl_status tl_load_solutions(tl_handle* h, const char* path, int* loaded)
         tl_gemm_solution s;
         memset(&s, 0, sizeof(s));
         float ms = 0;
-        if (sscanf(line.c_str() + b0, "[%d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %f", &s.kernel, &s.macro_tile0,
+        if (sscanf(line.c_str() + b0, "[%d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %f", &s.kernel, &s.macro_tile0,
                    &s.macro_tile1, &s.depth_u, &s.stages, &s.wave_tile0, &s.wave_tile1, &s.split_k, &s.raster, &s.ctas,
-                   &ms) == 11) {
+                   &s.promote_k, &ms) == 12) {
             std::lock_guard<std::mutex> g(h->mu);
             h->tuned[key] = s;
             ++n;
@@ -774,7 +811,8 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
     if (!h || !probs || !plan || count < 1 || !D || !A || !B) return fail(TL_ERR_INVALID_ARG, "NULL argument or count < 1");
     *plan = nullptr;
     const tl_gemm_problem& p0 = probs[0];
-    tl_status st;
+    tl_status st = bind_thread(h);
+    if (st != TL_SUCCESS) return st;
     for (int i = 0; i < count; ++i) {
         const tl_gemm_problem& p = probs[i];
         if ((st = validate(&p)) != TL_SUCCESS) return fail(st, "problem " + std::to_string(i) + ": " + g_last_error);

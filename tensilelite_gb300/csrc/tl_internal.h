@@ -80,6 +80,7 @@ struct TcLaunch {
     int split_k;
     int raster;
     int ctas;
+    int promote_k;           // k elements per TMEM accumulation chain of the A0*B0 product (0: whole k)
     // runtime
     int* err;
     uint64_t timeout_ns;

@@ -59,13 +59,16 @@ def kat_expected(M, N, K, pad):
     return D
 
 
-def make_case(dtype, layout, seed, m, n, k, alpha=1.0, beta=0.5):
+def make_case(dtype, layout, seed, m, n, k, alpha=1.0, beta=0.5, ld_align=1):
     """Seeded column-major buffers: A, B ~ N(0,1) drawn in that order, then C; cast to dtype (RNE).
-    Returns dict with storage bits, their exact fp32 values and leading dimensions."""
+    Leading dimensions are the stored row counts rounded up to ``ld_align`` elements (the padding
+    holds values too).  Returns dict with storage bits, their exact fp32 values and leading dims."""
     ta, tb = layout[0] == "T", layout[1] == "T"
     g = np.random.default_rng(seed)
     a_rows, a_cols = (k, m) if ta else (m, k)
     b_rows, b_cols = (n, k) if tb else (k, n)
+    a_rows = -(-a_rows // ld_align) * ld_align
+    b_rows = -(-b_rows // ld_align) * ld_align
     A = g.standard_normal(a_rows * a_cols)
     B = g.standard_normal(b_rows * b_cols)
     C = g.standard_normal(m * n)

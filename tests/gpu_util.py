@@ -44,7 +44,8 @@ def run_case(handle, case, kernel="auto", dtype=None, solution=None, rounding="r
     ldd = ldd or case["ldc"]
     A = to_dev(case["A_bits"], dt)
     B = to_dev(case["B_bits"], dt)
-    C = to_dev(case["C_bits"], od) if case["beta"] != 0 else None
+    C_bits = case["C_bits"] if od == case["out_dtype"] else orc.encode(case["C"], od)
+    C = to_dev(C_bits, od) if case["beta"] != 0 else None
     D = torch.full((ldd * n,), float("nan"), dtype=torch_dtype(od), device="cuda")
     p = tl.Problem.make(m, n, k, dtype=dt, out_dtype=od, trans_a=case["trans_a"], trans_b=case["trans_b"],
                         alpha=case["alpha"], beta=case["beta"], lda=case["lda"], ldb=case["ldb"], ldc=case["ldc"],
