@@ -170,6 +170,18 @@ TL_API tl_status tl_tune(tl_handle* handle, const tl_gemm_problem* problem, void
 /* Load tuned solutions from a JSON file written by tl_tune into the handle's cache. */
 TL_API tl_status tl_load_solutions(tl_handle* handle, const char* cache_path, int* loaded);
 
+/* The tcgen05 GEMM (split-k included) without any allocation, for callers that cannot call
+ * cudaMalloc: an application that owns all device memory through its own pool, a latency-critical
+ * path where an allocation (which may synchronise the device) is not acceptable, or a caller with no
+ * tl_handle (creating one allocates).  No counterpart in the reference.  Split-k partials, tile
+ * counters and the error word live in one static device array of 64 MiB per device (held until the
+ * process exits); problems whose workspace exceeds it are refused with TL_ERR_UNSUPPORTED.  All calls
+ * share that array: each clears the parts it uses, and calls that overlap on the GPU race.  The
+ * first call on a device looks the array up with that device current -- make it before any stream
+ * capture.  fp16/bf16/fp8 operands (TCGEN05 only); solution == NULL uses the heuristic. */
+TL_API tl_status tl_gemm_noalloc(const tl_gemm_problem* problem, const tl_gemm_solution* solution, void* D,
+                                 const void* C, const void* A, const void* B, void* stream);
+
 /* ---- grouped GEMM (one persistent launch over many independent problems) ---------------------- */
 
 typedef struct tl_grouped_plan tl_grouped_plan;

@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtensilelite_gb300.so")
 CLI = os.path.join(HERE, "tensilelite")
 
-SOURCES = ["gemm_tc.cu", "gemm_simt.cu", "aux_kernels.cu", "tl_api.cpp"]
+SOURCES = ["gemm_tc.cu", "gemm_simt.cu", "aux_kernels.cu", "tl_api.cpp", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I" + ROOT]
 

@@ -571,6 +571,63 @@ tl_status save_cache(const char* path, const std::string& key, const tl_gemm_sol
 }
 
 }  // namespace
+
+// Validation and launch description of a tcgen05 GEMM for a caller that supplies the scratch
+// itself (tl_gemm_noalloc).  Allocates nothing: it only checks the problem and the solution and
+// reports how much split-k workspace (bytes) and how many tile counters the launch needs.
+tl_status plan_tc_noalloc(int sm_count, size_t smem_optin, const tl_gemm_problem* prob, const tl_gemm_solution* sol,
+                          void* D, const void* C, const void* A, const void* B, TcLaunch* L, size_t* ws_bytes,
+                          size_t* counter_count)
+{
+    tl_status st = validate(prob);
+    if (st != TL_SUCCESS) return st;
+    const tl_gemm_problem& p = *prob;
+    if (p.kernel != TL_KERNEL_AUTO && p.kernel != TL_KERNEL_TCGEN05)
+        return fail(TL_ERR_UNSUPPORTED, "tl_gemm_noalloc runs the tcgen05 kernel only");
+    if (p.dtype_a != TL_DTYPE_FP16 && p.dtype_a != TL_DTYPE_BF16 && p.dtype_a != TL_DTYPE_FP8_E4M3)
+        return fail(TL_ERR_UNSUPPORTED, "tl_gemm_noalloc takes fp16, bf16 or fp8 operands");
+    if ((p.m && p.n) && !D) return fail(TL_ERR_INVALID_ARG, "D is NULL");
+    if (p.beta != 0.0f && !C && p.m && p.n) return fail(TL_ERR_INVALID_ARG, "C is NULL with beta != 0");
+    if (p.k > 0 && p.m > 0 && p.n > 0 && (!A || !B)) return fail(TL_ERR_INVALID_ARG, "A or B is NULL");
+    std::string why;
+    if (p.m > 0 && p.n > 0 && p.k > 0 && !tma_ok(p, A, B, &why)) return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel: " + why);
+    tl_handle dev;                 // host-side device description only; holds no device memory
+    dev.sm_count = sm_count;
+    dev.smem_optin = smem_optin;
+    tl_gemm_solution s;
+    if (sol) {
+        s = *sol;
+        if (s.kernel == TL_KERNEL_AUTO) s.kernel = TL_KERNEL_TCGEN05;
+        if (s.kernel != TL_KERNEL_TCGEN05) return fail(TL_ERR_UNSUPPORTED, "tl_gemm_noalloc: solution must be TCGEN05");
+    } else {
+        tc_heuristic(&dev, p, TL_KERNEL_TCGEN05, &s);
+    }
+    if ((st = check_tc_solution(&dev, p, s)) != TL_SUCCESS) return st;
+    const int64_t tiles = ((p.n + kTcTileN - 1) / kTcTileN) * ((p.m + s.macro_tile0 - 1) / s.macro_tile0) * p.batch;
+    *ws_bytes = (s.split_k > 1) ? static_cast<size_t>(tiles) * s.split_k * kTcTileN * s.macro_tile0 * sizeof(float) : 0;
+    *counter_count = (s.split_k > 1) ? static_cast<size_t>(tiles) : 0;
+    memset(L, 0, sizeof(*L));
+    L->in_dtype = p.dtype_a;
+    L->out_dtype = p.dtype_d;
+    L->out_trunc = p.out_rounding;
+    L->pieces = 1;
+    L->opM[0] = {A, p.m, p.lda, p.stride_a, m_mn_major(p) ? 1 : 0};
+    L->opN[0] = {B, p.n, p.ldb, p.stride_b, n_mn_major(p) ? 1 : 0};
+    L->M = p.m; L->N = p.n; L->K = p.k; L->batch = p.batch;
+    L->D = D; L->C = (p.beta != 0.0f) ? C : nullptr;
+    L->ldd = p.ldd; L->ldc = p.ldc; L->stride_d = p.stride_d; L->stride_c = p.stride_c;
+    L->alpha = p.alpha * scale_of(p.scale_a) * scale_of(p.scale_b);
+    L->beta = p.beta;
+    L->bm = s.macro_tile0;
+    L->stages = s.stages;
+    L->split_k = s.split_k;
+    L->raster = s.raster;
+    L->ctas = s.ctas;
+    L->promote_k = s.promote_k;
+    L->sm_count = sm_count;
+    return TL_SUCCESS;
+}
+
 }  // namespace tl
 
 using namespace tl;
