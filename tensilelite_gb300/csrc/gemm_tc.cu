@@ -49,6 +49,7 @@ struct TcKernelParams {
     int M, N, K, batch;
     float alpha, beta;
     int bm, stages, split_k, raster;
+    int tile_rows;                // n rows per tile: 128 (one CTA) or 256 (CTA pair)
     int nterms;                   // tensor-core products per k-block (1, or 3 / 6 for the fp32 split)
     uint8_t term_n[8], term_m[8]; // piece of B / of A used by each product (the last is A0*B0)
     int promote_kb;               // >0: the A0*B0 product restarts its TMEM chain every promote_kb
@@ -113,7 +114,7 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, Tile
         j.alpha = p.alpha;
         j.beta = p.beta;
         j.b = b;
-        j.n0 = in * kTcTileN;
+        j.n0 = in * p.tile_rows;
         j.m0 = jm * p.bm;
         j.kb0 = static_cast<int>((static_cast<int64_t>(split) * p.num_kb) / p.split_k);
         j.kb1 = static_cast<int>((static_cast<int64_t>(split + 1) * p.num_kb) / p.split_k);
@@ -141,7 +142,7 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, Tile
         j.alpha = e.alpha;
         j.beta = e.beta;
         j.b = 0;
-        j.n0 = in * kTcTileN;
+        j.n0 = in * p.tile_rows;
         j.m0 = jm * p.bm;
         j.kb0 = 0;
         j.kb1 = (e.K + p.kb_elems - 1) / p.kb_elems;
@@ -317,13 +318,32 @@ __device__ __forceinline__ void split_finish(const TcKernelParams& p, const Tile
     asm volatile("bar.sync 1, 128;" ::: "memory");   // last_flag is reused by the next tile
 }
 
-template <int KIND, typename TD>
+// Hand a drained TMEM buffer back to the MMA issuer: one arrival per epilogue warp, on the leader
+// CTA's barrier (a remote arrival when this CTA is the peer of a pair).
+template <int CG>
+__device__ __forceinline__ void release_tmem(uint64_t* bar, int lane)
+{
+    ptx::tc_fence_before();
+    __syncwarp();
+    if (lane == 0) {
+        if constexpr (CG == 2) ptx::mbar_arrive_cluster(ptx::mapa_shared(ptx::smem_u32(bar), 0));
+        else ptx::mbar_arrive(bar);
+    }
+}
+
+template <int KIND, typename TD, int CG>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_constant__ TcKernelParams p)
 {
+    // CG == 2: a cluster of two CTAs on two SMs works on one 256-row tile.  Each CTA stages its own
+    // 128 rows of the n-side operand and its half of the m-side operand; the leader (rank 0) issues
+    // the pair MMAs, whose accumulator rows 0-127 live in the leader's TMEM and 128-255 in the peer's.
+    // TMA completions of both CTAs land on the leader's full barriers, MMA completions are multicast
+    // to both CTAs, and both epilogues release the leader's TMEM buffers with remote arrivals.
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const uint32_t bmc = static_cast<uint32_t>(p.bm) / CG;            // m-side rows staged by this CTA
     const uint32_t tileN_bytes = kTcTileN * kTcRowBytes;
-    const uint32_t stage_bytes = tileN_bytes + static_cast<uint32_t>(p.bm) * kTcRowBytes;
+    const uint32_t stage_bytes = tileN_bytes + bmc * kTcRowBytes;
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(p.stages) * stage_bytes);
     uint64_t* empty = full + kTcMaxStages;
     uint64_t* tfull = empty + kTcMaxStages;     // main accumulator buffers (per tile, or per chain)
@@ -336,22 +356,27 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
+    const uint32_t rank = (CG == 2) ? ptx::cluster_ctarank() : 0u;
+    const bool leader = (rank == 0);
+    const int64_t unit0 = (CG == 2) ? static_cast<int64_t>(ptx::cluster_id_x()) : static_cast<int64_t>(blockIdx.x);
+    const int64_t units = (CG == 2) ? static_cast<int64_t>(ptx::ncluster_x()) : static_cast<int64_t>(gridDim.x);
     const bool promo = p.promote_kb > 0;
     const bool sep_small = promo && p.nterms > 1;
     // TMEM columns: main accumulator x2 (+ small-term accumulator x2 when they are kept apart)
     const uint32_t need_cols = static_cast<uint32_t>(p.bm) * (sep_small ? 4u : 2u);
     const uint32_t tmem_cols = need_cols <= 128 ? 128u : (need_cols <= 256 ? 256u : 512u);
+    const uint32_t epi_arrivals = 4u * CG;     // one per epilogue warp of each CTA
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < p.stages; ++s) {
-            ptx::mbar_init(&full[s], 1);
+            ptx::mbar_init(&full[s], CG);
             ptx::mbar_init(&empty[s], 1);
         }
         for (int a = 0; a < 2; ++a) {
             ptx::mbar_init(&tfull[a], 1);
-            ptx::mbar_init(&tempty[a], 128);
+            ptx::mbar_init(&tempty[a], epi_arrivals);
             ptx::mbar_init(&sfull[a], 1);
-            ptx::mbar_init(&sempty[a], 128);
+            ptx::mbar_init(&sempty[a], epi_arrivals);
         }
         *abort_flag = 0;
         *last_flag = 0;
@@ -359,8 +384,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
         ptx::fence_proxy_async_smem();
     }
     if (warp == 1) {
-        ptx::tmem_alloc(tmem_slot, tmem_cols);
-        ptx::tmem_relinquish();
+        if constexpr (CG == 2) {
+            ptx::tmem_alloc_pair(tmem_slot, tmem_cols);
+            ptx::tmem_relinquish_pair();
+        } else {
+            ptx::tmem_alloc(tmem_slot, tmem_cols);
+            ptx::tmem_relinquish();
+        }
     }
     if (warp == 0 && lane == 0 && p.group == nullptr) {
         for (int v = 0; v < p.nterms; ++v) {
@@ -370,20 +400,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
     }
     ptx::tc_fence_before();
     __syncthreads();
+    if constexpr (CG == 2) ptx::cluster_sync();     // peer barriers initialised before any remote arrive
     ptx::tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
     const int nvirt = p.nterms;
     const uint64_t tlim = p.timeout_ns;
 
     if (warp == 0) {
-        // ------------------------------------------------------------------ TMA producer
+        // ------------------------------------------------------------------ TMA producer (each CTA)
         if (lane == 0) {
             uint32_t stage = 0, phase = 0;
             const int W = kTcRowBytes / (KIND == 0 ? 2 : 1);   // elements per 128-byte row
             bool ok = true;
-            for (int64_t w = blockIdx.x; w < p.total_work && ok; w += gridDim.x) {
+            for (int64_t w = unit0; w < p.total_work && ok; w += units) {
                 TileJob j;
                 get_job(p, w, j);
+                const int n0 = j.n0 + static_cast<int>(rank) * kTcTileN;
+                const int m0 = j.m0 + static_cast<int>(rank * bmc);
                 for (int kb = j.kb0; kb < j.kb1 && ok; ++kb) {
                     for (int v = 0; v < nvirt; ++v) {
                         if (!ptx::mbar_wait(&empty[stage], phase ^ 1u, tlim, abort_flag)) {
@@ -396,19 +429,36 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         // split-precision products, smallest first (term table set by the host)
                         const void* mapN = p.group ? j.tmN : static_cast<const void*>(&p.tmN[p.term_n[v]]);
                         const void* mapM = p.group ? j.tmM : static_cast<const void*>(&p.tmM[p.term_m[v]]);
-                        ptx::mbar_arrive_expect_tx(&full[stage], stage_bytes);
                         const int k0 = kb * W;
-                        if (!p.n_mn_major) {
-                            ptx::tma_load_3d(sN, mapN, &full[stage], k0, j.n0, j.b);
+                        if constexpr (CG == 2) {
+                            const uint32_t fb = ptx::mapa_shared(ptx::smem_u32(&full[stage]), 0);
+                            ptx::mbar_arrive_expect_tx_cluster(fb, stage_bytes);
+                            if (!p.n_mn_major) {
+                                ptx::tma_load_3d_pair(sN, mapN, fb, k0, n0, j.b);
+                            } else {
+                                for (int c = 0; c < kTcTileN / W; ++c)
+                                    ptx::tma_load_3d_pair(sN + c * W * kTcRowBytes, mapN, fb, n0 + c * W, k0, j.b);
+                            }
+                            if (!p.m_mn_major) {
+                                ptx::tma_load_3d_pair(sM, mapM, fb, k0, m0, j.b);
+                            } else {
+                                for (int c = 0; c < static_cast<int>(bmc) / W; ++c)
+                                    ptx::tma_load_3d_pair(sM + c * W * kTcRowBytes, mapM, fb, m0 + c * W, k0, j.b);
+                            }
                         } else {
-                            for (int c = 0; c < kTcTileN / W; ++c)
-                                ptx::tma_load_3d(sN + c * W * kTcRowBytes, mapN, &full[stage], j.n0 + c * W, k0, j.b);
-                        }
-                        if (!p.m_mn_major) {
-                            ptx::tma_load_3d(sM, mapM, &full[stage], k0, j.m0, j.b);
-                        } else {
-                            for (int c = 0; c < p.bm / W; ++c)
-                                ptx::tma_load_3d(sM + c * W * kTcRowBytes, mapM, &full[stage], j.m0 + c * W, k0, j.b);
+                            ptx::mbar_arrive_expect_tx(&full[stage], stage_bytes);
+                            if (!p.n_mn_major) {
+                                ptx::tma_load_3d(sN, mapN, &full[stage], k0, n0, j.b);
+                            } else {
+                                for (int c = 0; c < kTcTileN / W; ++c)
+                                    ptx::tma_load_3d(sN + c * W * kTcRowBytes, mapN, &full[stage], n0 + c * W, k0, j.b);
+                            }
+                            if (!p.m_mn_major) {
+                                ptx::tma_load_3d(sM, mapM, &full[stage], k0, m0, j.b);
+                            } else {
+                                for (int c = 0; c < static_cast<int>(bmc) / W; ++c)
+                                    ptx::tma_load_3d(sM + c * W * kTcRowBytes, mapM, &full[stage], m0 + c * W, k0, j.b);
+                            }
                         }
                         if (++stage == static_cast<uint32_t>(p.stages)) {
                             stage = 0;
@@ -419,16 +469,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             }
         }
     } else if (warp == 1) {
-        // ------------------------------------------------------------------ MMA issuer
+        // ------------------------------------------------------------------ MMA issuer (leader CTA)
         // Without promotion a tile's whole k range accumulates in one TMEM buffer (two buffers
         // alternate between tiles).  With promotion the A0*B0 product restarts its accumulation
         // every promote_kb k-blocks in the alternate buffer (the epilogue drains each chain into
         // fp32 registers), and the small split-precision products accumulate for the whole tile in
         // a separate pair of buffers.
-        if (lane == 0) {
+        if (lane == 0 && leader) {
             uint32_t stage = 0, phase = 0, mbuf = 0, mph = 0, sbuf = 0, sph = 0;
             bool ok = true;
-            for (int64_t w = blockIdx.x; w < p.total_work && ok; w += gridDim.x) {
+            for (int64_t w = unit0; w < p.total_work && ok; w += units) {
                 TileJob j;
                 get_job(p, w, j);
                 const int nkb = j.kb1 - j.kb0;
@@ -469,12 +519,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                                 const uint64_t adesc = ptx::sdesc_sw128(sN + ks * p.n_kstep, p.n_lbo, 1024);
                                 const uint64_t bdesc = ptx::sdesc_sw128(sM + ks * p.m_kstep, p.m_lbo, 1024);
                                 const uint32_t accumulate = (started || ks > 0) ? 1u : 0u;
-                                if (KIND == 0) ptx::mma_f16(d_tmem, adesc, bdesc, p.idesc, accumulate);
-                                else ptx::mma_f8(d_tmem, adesc, bdesc, p.idesc, accumulate);
+                                if constexpr (CG == 2) {
+                                    if (KIND == 0) ptx::mma_f16_pair(d_tmem, adesc, bdesc, p.idesc, accumulate);
+                                    else ptx::mma_f8_pair(d_tmem, adesc, bdesc, p.idesc, accumulate);
+                                } else {
+                                    if (KIND == 0) ptx::mma_f16(d_tmem, adesc, bdesc, p.idesc, accumulate);
+                                    else ptx::mma_f8(d_tmem, adesc, bdesc, p.idesc, accumulate);
+                                }
                             }
                             if (is_main) main_started = true;
                             else small_started = true;
-                            ptx::mma_commit(&empty[stage]);
+                            if constexpr (CG == 2) ptx::mma_commit_pair(&empty[stage], 0x3);
+                            else ptx::mma_commit(&empty[stage]);
                             if (++stage == static_cast<uint32_t>(p.stages)) {
                                 stage = 0;
                                 phase ^= 1u;
@@ -482,33 +538,37 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         }
                     }
                     if (!ok) break;
-                    ptx::mma_commit(&tfull[mbuf]);
+                    if constexpr (CG == 2) ptx::mma_commit_pair(&tfull[mbuf], 0x3);
+                    else ptx::mma_commit(&tfull[mbuf]);
                     mbuf ^= 1u;
                     if (mbuf == 0) mph ^= 1u;
                 }
                 if (!ok) break;
                 if (sep_small) {
-                    ptx::mma_commit(&sfull[sbuf]);
+                    if constexpr (CG == 2) ptx::mma_commit_pair(&sfull[sbuf], 0x3);
+                    else ptx::mma_commit(&sfull[sbuf]);
                     sbuf ^= 1u;
                     if (sbuf == 0) sph ^= 1u;
                 }
             }
         }
     } else {
-        // ------------------------------------------------------------------ epilogue (4 warps)
+        // ------------------------------------------------------------------ epilogue (4 warps, each CTA)
         // All four warps run the same loop and, in split-k mode, the same named barriers: after a
         // timed-out wait a warp keeps the control flow and only skips the work, so no warp can be
         // left waiting at bar.sync 1 for one that gave up.
         const int quarter = warp & 3;             // TMEM lanes 32*quarter .. +31
-        const int row = quarter * 32 + lane;      // tile row = problem n offset
+        const int row = quarter * 32 + lane;      // tile row = problem n offset within this CTA
         const int et = threadIdx.x - 64;          // 0..127
         const uint32_t lane_off = static_cast<uint32_t>(quarter * 32) << 16;
         uint32_t mbuf = 0, mph = 0, sbuf = 0, sph = 0;
         const int chunks = p.bm / 32;
         bool ok = true;
-        for (int64_t w = blockIdx.x; w < p.total_work; w += gridDim.x) {
+        for (int64_t w = unit0; w < p.total_work; w += units) {
             TileJob j;
             get_job(p, w, j);
+            j.n0 += static_cast<int>(rank) * kTcTileN;
+            j.tile = j.tile * CG + rank;              // split-k slabs and counters per CTA half
             const int n = j.n0 + row;
             const bool row_ok = n < j.N;
             const int64_t base_d = static_cast<int64_t>(j.b) * p.stride_d + static_cast<int64_t>(n) * j.ldd;
@@ -538,8 +598,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
 #pragma unroll
                             for (int i = 0; i < 32; ++i) run[q * 32 + i] += __uint_as_float(r[i]);
                         }
-                        ptx::tc_fence_before();
-                        ptx::mbar_arrive(&tempty[mbuf]);
+                        release_tmem<CG>(&tempty[mbuf], lane);
                     }
                     mbuf ^= 1u;
                     if (mbuf == 0) mph ^= 1u;
@@ -562,8 +621,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
 #pragma unroll
                             for (int i = 0; i < 32; ++i) run[q * 32 + i] += __uint_as_float(r[i]);
                         }
-                        ptx::tc_fence_before();
-                        ptx::mbar_arrive(&sempty[sbuf]);
+                        release_tmem<CG>(&sempty[sbuf], lane);
                     }
                     sbuf ^= 1u;
                     if (sbuf == 0) sph ^= 1u;
@@ -610,10 +668,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                     uint32_t r[32];
                     __syncwarp();
                     ptx::tmem_ld32(tbase + c * 32, r);
-                    if (c == chunks - 1) {
-                        ptx::tc_fence_before();
-                        ptx::mbar_arrive(&tempty[mbuf]);
-                    }
+                    if (c == chunks - 1) release_tmem<CG>(&tempty[mbuf], lane);
                     const int m = j.m0 + c * 32;
                     if (row_ok && m < j.M) {
                         float v[32];
@@ -630,10 +685,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                     uint32_t r[32];
                     __syncwarp();
                     ptx::tmem_ld32(tbase + c * 32, r);
-                    if (c == chunks - 1) {
-                        ptx::tc_fence_before();
-                        ptx::mbar_arrive(&tempty[mbuf]);
-                    }
+                    if (c == chunks - 1) release_tmem<CG>(&tempty[mbuf], lane);
                     float4* dst = reinterpret_cast<float4*>(slab + (static_cast<size_t>(c) * kTcTileN + row) * 32);
 #pragma unroll
                     for (int q = 0; q < 8; ++q)
@@ -649,9 +701,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
 
     ptx::tc_fence_before();
     __syncthreads();
+    if constexpr (CG == 2) ptx::cluster_sync();     // no remote arrival or pair MMA still targets us
     if (warp == 1) {
         ptx::tc_fence_after();
-        ptx::tmem_dealloc(tmem_base, tmem_cols);
+        if constexpr (CG == 2) ptx::tmem_dealloc_pair(tmem_base, tmem_cols);
+        else ptx::tmem_dealloc(tmem_base, tmem_cols);
     }
 }
 
@@ -675,38 +729,118 @@ EncodeTiledFn get_encode_fn()
     return fn;
 }
 
-template <int KIND, typename TD>
+template <int KIND, typename TD, int CG>
 tl_status launch_kernel(const TcKernelParams& kp, int grid, size_t smem, cudaStream_t stream)
 {
-    auto kern = tc_gemm_kernel<KIND, TD>;
+    auto kern = tc_gemm_kernel<KIND, TD, CG>;
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;
     std::call_once(once, [&] {
         attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     });
     if (attr_err != cudaSuccess) return cuda_fail(attr_err, "cudaFuncSetAttribute(tc_gemm_kernel)");
-    kern<<<grid, kTcThreads, smem, stream>>>(kp);
+    if constexpr (CG == 1) {
+        kern<<<grid, kTcThreads, smem, stream>>>(kp);
+    } else {
+        cudaLaunchConfig_t cfg;
+        memset(&cfg, 0, sizeof(cfg));
+        cfg.gridDim = dim3(static_cast<unsigned>(grid), 1, 1);
+        cfg.blockDim = dim3(kTcThreads, 1, 1);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 2;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cudaError_t e = cudaLaunchKernelEx(&cfg, kern, kp);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchKernelEx(tc_gemm_kernel, cluster of 2)");
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "tc_gemm_kernel launch");
     return TL_SUCCESS;
 }
 
-tl_status dispatch(int in_dtype, int out_dtype, const TcKernelParams& kp, int grid, size_t smem, cudaStream_t s)
+// Number of clusters of two that can be resident at once with this shared-memory size (cached).
+template <int KIND, typename TD>
+int max_pair_clusters(size_t smem)
+{
+    static std::mutex mu;
+    static std::map<size_t, int> cache;
+    std::lock_guard<std::mutex> g(mu);
+    auto it = cache.find(smem);
+    if (it != cache.end()) return it->second;
+    auto kern = tc_gemm_kernel<KIND, TD, 2>;
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(2, 1, 1);
+    cfg.blockDim = dim3(kTcThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        n = 0;
+    }
+    cache[smem] = n;
+    return n;
+}
+
+template <int CG>
+tl_status dispatch_cg(int in_dtype, int out_dtype, const TcKernelParams& kp, int grid, size_t smem, cudaStream_t s)
 {
     const int kind = (in_dtype == TL_DTYPE_FP8_E4M3) ? 1 : 0;
     if (kind == 0) {
-        if (out_dtype == TL_DTYPE_FP32) return launch_kernel<0, float>(kp, grid, smem, s);
-        if (out_dtype == TL_DTYPE_FP16) return launch_kernel<0, __half>(kp, grid, smem, s);
-        if (out_dtype == TL_DTYPE_BF16) return launch_kernel<0, __nv_bfloat16>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_FP32) return launch_kernel<0, float, CG>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_FP16) return launch_kernel<0, __half, CG>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_BF16) return launch_kernel<0, __nv_bfloat16, CG>(kp, grid, smem, s);
     } else {
-        if (out_dtype == TL_DTYPE_FP32) return launch_kernel<1, float>(kp, grid, smem, s);
-        if (out_dtype == TL_DTYPE_FP16) return launch_kernel<1, __half>(kp, grid, smem, s);
-        if (out_dtype == TL_DTYPE_BF16) return launch_kernel<1, __nv_bfloat16>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_FP32) return launch_kernel<1, float, CG>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_FP16) return launch_kernel<1, __half, CG>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_BF16) return launch_kernel<1, __nv_bfloat16, CG>(kp, grid, smem, s);
     }
     return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel: unsupported output type");
 }
 
-uint32_t make_idesc(int in_dtype, int n_mn_major, int m_mn_major, int bm)
+// Grid: one CTA per SM (CG 1) or as many co-resident pairs as fit (CG 2), never more than the work.
+tl_status dispatch(int in_dtype, int out_dtype, int cg, const TcKernelParams& kp, int ctas, int sm_count,
+                   int64_t total_work, size_t smem, cudaStream_t s)
+{
+    if (cg == 1) {
+        int grid = ctas > 0 ? ctas : sm_count;
+        if (grid > total_work) grid = static_cast<int>(total_work);
+        if (grid < 1) grid = 1;
+        return dispatch_cg<1>(in_dtype, out_dtype, kp, grid, smem, s);
+    }
+    int pairs = ctas > 0 ? ctas / 2 : 0;
+    if (pairs <= 0) {
+        const int kind = (in_dtype == TL_DTYPE_FP8_E4M3) ? 1 : 0;
+        int maxc = 0;
+        if (kind == 0)
+            maxc = out_dtype == TL_DTYPE_FP32   ? max_pair_clusters<0, float>(smem)
+                   : out_dtype == TL_DTYPE_FP16 ? max_pair_clusters<0, __half>(smem)
+                                                : max_pair_clusters<0, __nv_bfloat16>(smem);
+        else
+            maxc = out_dtype == TL_DTYPE_FP32   ? max_pair_clusters<1, float>(smem)
+                   : out_dtype == TL_DTYPE_FP16 ? max_pair_clusters<1, __half>(smem)
+                                                : max_pair_clusters<1, __nv_bfloat16>(smem);
+        pairs = maxc > 0 ? maxc : sm_count / 2;
+    }
+    if (pairs > total_work) pairs = static_cast<int>(total_work);
+    if (pairs < 1) pairs = 1;
+    return dispatch_cg<2>(in_dtype, out_dtype, kp, 2 * pairs, smem, s);
+}
+
+uint32_t make_idesc(int in_dtype, int n_mn_major, int m_mn_major, int bm, int cg)
 {
     uint32_t d = 1u << 4;                                  // accumulator F32
     uint32_t t = (in_dtype == TL_DTYPE_BF16) ? 1u : 0u;    // kind::f16: 0 F16, 1 BF16; f8f6f4: 0 E4M3
@@ -715,7 +849,7 @@ uint32_t make_idesc(int in_dtype, int n_mn_major, int m_mn_major, int bm)
     d |= static_cast<uint32_t>(n_mn_major & 1) << 15;      // A major: 0 K, 1 MN
     d |= static_cast<uint32_t>(m_mn_major & 1) << 16;      // B major
     d |= static_cast<uint32_t>(bm >> 3) << 17;             // N >> 3
-    d |= static_cast<uint32_t>(kTcTileN >> 4) << 24;       // M >> 4
+    d |= static_cast<uint32_t>((kTcTileN * cg) >> 4) << 24;  // M >> 4 (256 for a CTA pair)
     return d;
 }
 
@@ -795,9 +929,10 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     memset(&kp, 0, sizeof(kp));
     tl_status st;
     const int pieces = L.pieces < 1 ? 1 : L.pieces;
+    const int cg = L.cg == 2 ? 2 : 1;
     for (int i = 0; i < pieces; ++i) {
         if ((st = tc_encode_operand(&kp.tmN[i], L.in_dtype, L.opN[i], L.K, L.batch, kTcTileN)) != TL_SUCCESS) return st;
-        if ((st = tc_encode_operand(&kp.tmM[i], L.in_dtype, L.opM[i], L.K, L.batch, L.bm)) != TL_SUCCESS) return st;
+        if ((st = tc_encode_operand(&kp.tmM[i], L.in_dtype, L.opM[i], L.K, L.batch, L.bm / cg)) != TL_SUCCESS) return st;
     }
     // products per k-block, smallest first: 2-piece split -> A1B0, A0B1, A0B0;
     // 3-piece split -> A2B0, A1B1, A0B2, A1B0, A0B1, A0B0
@@ -825,14 +960,15 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     kp.split_k = L.split_k;
     kp.raster = L.raster;
     kp.tiles_m = static_cast<int>((L.M + L.bm - 1) / L.bm);
-    kp.tiles_n = static_cast<int>((L.N + kTcTileN - 1) / kTcTileN);
+    kp.tile_rows = kTcTileN * cg;
+    kp.tiles_n = static_cast<int>((L.N + kp.tile_rows - 1) / kp.tile_rows);
     kp.num_kb = static_cast<int>((L.K + W - 1) / W);
     kp.kb_elems = W;
     kp.promote_kb = L.promote_k > 0 ? static_cast<int>((L.promote_k + W - 1) / W) : 0;
     kp.total_work = static_cast<int64_t>(kp.tiles_m) * kp.tiles_n * L.batch * L.split_k;
     kp.n_mn_major = L.opN[0].mn_major;
     kp.m_mn_major = L.opM[0].mn_major;
-    kp.idesc = make_idesc(L.in_dtype, kp.n_mn_major, kp.m_mn_major, L.bm);
+    kp.idesc = make_idesc(L.in_dtype, kp.n_mn_major, kp.m_mn_major, L.bm, cg);
     desc_params(L.in_dtype, kp.n_mn_major, kp.n_lbo, kp.n_kstep);
     desc_params(L.in_dtype, kp.m_mn_major, kp.m_lbo, kp.m_kstep);
     kp.out_trunc = L.out_trunc;
@@ -840,11 +976,8 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     kp.counters = L.counters;
     kp.err = L.err;
     kp.timeout_ns = L.timeout_ns;
-    int grid = L.ctas > 0 ? L.ctas : L.sm_count;
-    if (grid > kp.total_work) grid = static_cast<int>(kp.total_work);
-    if (grid < 1) grid = 1;
-    const size_t smem = tc_smem_bytes(L.bm, L.stages);
-    st = dispatch(L.in_dtype, L.out_dtype, kp, grid, smem, stream);
+    const size_t smem = tc_smem_bytes(L.bm / cg, L.stages);
+    st = dispatch(L.in_dtype, L.out_dtype, cg, kp, L.ctas, L.sm_count, kp.total_work, smem, stream);
     if (st == TL_SUCCESS && launches) ++*launches;
     return st;
 }
@@ -866,17 +999,16 @@ tl_status tc_grouped_launch(const TcGroupLaunch& G, cudaStream_t stream, int64_t
     kp.stride_d = 0;
     kp.n_mn_major = G.n_mn_major;
     kp.m_mn_major = G.m_mn_major;
-    kp.idesc = make_idesc(G.in_dtype, G.n_mn_major, G.m_mn_major, G.bm);
+    const int cg = G.cg == 2 ? 2 : 1;
+    kp.tile_rows = kTcTileN * cg;
+    kp.idesc = make_idesc(G.in_dtype, G.n_mn_major, G.m_mn_major, G.bm, cg);
     desc_params(G.in_dtype, G.n_mn_major, kp.n_lbo, kp.n_kstep);
     desc_params(G.in_dtype, G.m_mn_major, kp.m_lbo, kp.m_kstep);
     kp.out_trunc = G.out_trunc;
     kp.err = G.err;
     kp.timeout_ns = G.timeout_ns;
-    int grid = G.ctas > 0 ? G.ctas : G.sm_count;
-    if (grid > G.total_tiles) grid = static_cast<int>(G.total_tiles);
-    if (grid < 1) grid = 1;
-    const size_t smem = tc_smem_bytes(G.bm, G.stages);
-    tl_status st = dispatch(G.in_dtype, G.out_dtype, kp, grid, smem, stream);
+    const size_t smem = tc_smem_bytes(G.bm / cg, G.stages);
+    tl_status st = dispatch(G.in_dtype, G.out_dtype, cg, kp, G.ctas, G.sm_count, G.total_tiles, smem, stream);
     if (st == TL_SUCCESS && launches) ++*launches;
     return st;
 }

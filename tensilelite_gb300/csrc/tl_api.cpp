@@ -151,10 +151,10 @@ int resolve_kernel(const tl_gemm_problem& p)
     return p.dtype_a == TL_DTYPE_FP32 ? TL_KERNEL_SIMT : TL_KERNEL_TCGEN05;
 }
 
-int max_stages(int bm, size_t smem_optin)
+int max_stages(int bm_cta, size_t smem_optin)
 {
     int s = kTcMaxStages;
-    while (s > 2 && tc_smem_bytes(bm, s) > smem_optin) --s;
+    while (s > 2 && tc_smem_bytes(bm_cta, s) > smem_optin) --s;
     return s;
 }
 
@@ -210,10 +210,16 @@ void tc_heuristic(const tl_handle* h, const tl_gemm_problem& p, int kernel, tl_g
             split = std::max(1, static_cast<int>(std::min<int64_t>(std::min<int64_t>(h->sm_count / std::max<int64_t>(1, t128),
                                                                                      num_kb / 4), 16)));
     }
+    int cg = 1;
+    if (!is_split(kernel) && bm == 256 && split == 1) {
+        // large problems: a CTA pair per 256 x 256 tile halves the n-side operand each SM stages
+        const int64_t pair_tiles = ((p.n + 2 * kTcTileN - 1) / (2 * kTcTileN)) * ((p.m + 255) / 256) * p.batch;
+        if (pair_tiles >= h->sm_count / 2 && (!mmn || (bm / 2) % W == 0)) cg = 2;
+    }
     s->macro_tile0 = bm;
-    s->macro_tile1 = kTcTileN;
+    s->macro_tile1 = kTcTileN * cg;
     s->depth_u = W;
-    s->stages = max_stages(bm, h->smem_optin);
+    s->stages = max_stages(bm / cg, h->smem_optin);
     s->wave_tile0 = 0;
     s->wave_tile1 = 0;
     s->split_k = split;
@@ -227,15 +233,20 @@ tl_status check_tc_solution(const tl_handle* h, const tl_gemm_problem& p, const 
     if (in != TL_DTYPE_FP16 && in != TL_DTYPE_BF16 && in != TL_DTYPE_FP8_E4M3)
         return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel needs fp16, bf16 or fp8 operands");
     const int W = row_elems(in);
-    if (s.macro_tile1 != kTcTileN) return fail(TL_ERR_UNSUPPORTED, "macro_tile1 (n) must be 128 for tcgen05");
+    if (s.macro_tile1 != kTcTileN && s.macro_tile1 != 2 * kTcTileN)
+        return fail(TL_ERR_UNSUPPORTED, "macro_tile1 (n) must be 128 (one SM) or 256 (a CTA pair) for tcgen05");
+    const int cg = s.macro_tile1 / kTcTileN;
     const int bm = s.macro_tile0;
     if (bm != 64 && bm != 128 && bm != 192 && bm != 256)
         return fail(TL_ERR_UNSUPPORTED, "macro_tile0 (m) must be 64, 128, 192 or 256");
+    if (cg == 2 && bm != 128 && bm != 256)
+        return fail(TL_ERR_UNSUPPORTED, "a CTA pair (macro_tile1 256) needs macro_tile0 128 or 256");
     const bool mmn = m_mn_major(p);
-    if (mmn && bm % W) return fail(TL_ERR_UNSUPPORTED, "macro_tile0 must be a multiple of the 128-byte row for MN-major A");
+    if (mmn && (bm / cg) % W)
+        return fail(TL_ERR_UNSUPPORTED, "m rows per CTA must be a multiple of the 128-byte row for MN-major A");
     if (s.depth_u != 0 && s.depth_u != W) return fail(TL_ERR_UNSUPPORTED, "depth_u is fixed to one 128-byte row");
     if (s.stages < 2 || s.stages > kTcMaxStages) return fail(TL_ERR_UNSUPPORTED, "stages must be in [2, 8]");
-    if (tc_smem_bytes(bm, s.stages) > h->smem_optin) return fail(TL_ERR_UNSUPPORTED, "shared memory budget exceeded");
+    if (tc_smem_bytes(bm / cg, s.stages) > h->smem_optin) return fail(TL_ERR_UNSUPPORTED, "shared memory budget exceeded");
     const int64_t num_kb = (p.k + W - 1) / W;
     if (s.split_k < 1 || (num_kb > 0 && s.split_k > num_kb) || s.split_k > 64)
         return fail(TL_ERR_UNSUPPORTED, "split_k must be in [1, min(64, k blocks)]");
@@ -404,7 +415,9 @@ tl_status prepare(tl_handle* h, const tl_gemm_problem* prob, const tl_gemm_solut
     }
     const int W = row_elems(tc_in_dtype(p));
     (void)W;
-    const int64_t tiles = ((p.n + kTcTileN - 1) / kTcTileN) * ((p.m + P.s.macro_tile0 - 1) / P.s.macro_tile0) * p.batch;
+    const int cgp = P.s.macro_tile1 / kTcTileN;
+    const int64_t tiles = ((p.n + kTcTileN * cgp - 1) / (kTcTileN * cgp)) * cgp *
+                          ((p.m + P.s.macro_tile0 - 1) / P.s.macro_tile0) * p.batch;
     if (P.s.split_k > 1) {
         off_part = need;
         need = off_part + static_cast<size_t>(tiles) * P.s.split_k * kTcTileN * P.s.macro_tile0 * sizeof(float);
@@ -485,6 +498,7 @@ tl_status enqueue(tl_handle* h, const Prepared& P, cudaStream_t s)
     L.raster = P.s.raster;
     L.ctas = P.s.ctas;
     L.promote_k = P.s.promote_k;
+    L.cg = P.s.macro_tile1 / kTcTileN;
     L.err = h->d_err;
     L.timeout_ns = h->timeout_ns;
     L.workspace = P.ws_partials;
@@ -501,6 +515,7 @@ std::vector<tl_gemm_solution> tc_candidates(const tl_handle* h, const tl_gemm_pr
     const int W = row_elems(in);
     const int64_t num_kb = std::max<int64_t>(1, (p.k + W - 1) / W);
     const int64_t tiles_n = (p.n + kTcTileN - 1) / kTcTileN;
+    for (int cg : {1, 2})
     for (int bm : {64, 128, 192, 256}) {
         for (int split : {1, 2, 3, 4, 6, 8, 12, 16}) {
             if (split > num_kb) continue;
@@ -509,9 +524,9 @@ std::vector<tl_gemm_solution> tc_candidates(const tl_handle* h, const tl_gemm_pr
                 memset(&s, 0, sizeof(s));
                 s.kernel = kernel;
                 s.macro_tile0 = bm;
-                s.macro_tile1 = kTcTileN;
+                s.macro_tile1 = kTcTileN * cg;
                 s.depth_u = W;
-                s.stages = max_stages(bm, h->smem_optin);
+                s.stages = max_stages(bm / cg, h->smem_optin);
                 s.split_k = split;
                 s.raster = raster;
                 if (is_split(kernel)) s.promote_k = 256;
@@ -519,10 +534,12 @@ std::vector<tl_gemm_solution> tc_candidates(const tl_handle* h, const tl_gemm_pr
                 if (check_tc_solution(h, p, s) != TL_SUCCESS) continue;
                 // cost model: tensor work per tile grows with bm (efficiency of the 128 x bm MMA),
                 // waves quantise, split-k adds a partial round trip
-                const int64_t tiles = tiles_n * ((p.m + bm - 1) / bm) * p.batch;
+                const int64_t tiles = ((p.n + kTcTileN * cg - 1) / (kTcTileN * cg)) * ((p.m + bm - 1) / bm) * p.batch;
                 const int64_t work = tiles * split;
-                const double waves = std::ceil(static_cast<double>(work) / h->sm_count);
-                const double per_unit = (static_cast<double>(bm) / 256.0 + 0.15) * (static_cast<double>(num_kb) / split + 4.0);
+                const double waves = std::ceil(static_cast<double>(work) / (h->sm_count / cg));
+                // per work unit: MMA time grows with the tile; a CTA pair stages half the n operand per SM
+                const double per_unit = (static_cast<double>(bm) / 256.0 + 0.15) * (cg == 2 ? 0.85 : 1.0) *
+                                        (static_cast<double>(num_kb) / split + 4.0);
                 double cost = waves * per_unit;
                 if (split > 1) cost *= 1.0 + 0.02 * split;
                 if (raster == 0 && tiles_n > 8) cost *= 1.02;
@@ -603,7 +620,9 @@ tl_status plan_tc_noalloc(int sm_count, size_t smem_optin, const tl_gemm_problem
         tc_heuristic(&dev, p, TL_KERNEL_TCGEN05, &s);
     }
     if ((st = check_tc_solution(&dev, p, s)) != TL_SUCCESS) return st;
-    const int64_t tiles = ((p.n + kTcTileN - 1) / kTcTileN) * ((p.m + s.macro_tile0 - 1) / s.macro_tile0) * p.batch;
+    const int cgp = s.macro_tile1 / kTcTileN;
+    const int64_t tiles = ((p.n + kTcTileN * cgp - 1) / (kTcTileN * cgp)) * cgp *
+                          ((p.m + s.macro_tile0 - 1) / s.macro_tile0) * p.batch;
     *ws_bytes = (s.split_k > 1) ? static_cast<size_t>(tiles) * s.split_k * kTcTileN * s.macro_tile0 * sizeof(float) : 0;
     *counter_count = (s.split_k > 1) ? static_cast<size_t>(tiles) : 0;
     memset(L, 0, sizeof(*L));
@@ -624,6 +643,7 @@ tl_status plan_tc_noalloc(int sm_count, size_t smem_optin, const tl_gemm_problem
     L->raster = s.raster;
     L->ctas = s.ctas;
     L->promote_k = s.promote_k;
+    L->cg = cgp;
     L->sm_count = sm_count;
     return TL_SUCCESS;
 }
@@ -899,7 +919,7 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
         med.kernel = TL_KERNEL_TCGEN05;
         tc_heuristic(h, med, TL_KERNEL_TCGEN05, &s);
         s.macro_tile0 = 256;
-        if (m_mn_major(p0) && p0.dtype_a == TL_DTYPE_FP8_E4M3) s.macro_tile0 = 256;
+        s.macro_tile1 = kTcTileN;
         s.stages = max_stages(s.macro_tile0, h->smem_optin);
         s.split_k = 1;
         s.raster = 0;
@@ -920,7 +940,9 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
         TcOperand opM{A[i], p.m, p.lda, p.stride_a, m_mn_major(p) ? 1 : 0};
         if (p.m > 0 && p.n > 0) {
             if ((st = tc_encode_operand(&e.tmN, p.dtype_a, opN, p.k, 1, kTcTileN)) != TL_SUCCESS) return st;
-            if ((st = tc_encode_operand(&e.tmM, p.dtype_a, opM, p.k, 1, s.macro_tile0)) != TL_SUCCESS) return st;
+            if ((st = tc_encode_operand(&e.tmM, p.dtype_a, opM, p.k, 1, s.macro_tile0 * kTcTileN / s.macro_tile1)) !=
+                TL_SUCCESS)
+                return st;
         }
         e.D = D[i];
         e.C = (p.beta != 0.0f && C) ? C[i] : nullptr;
@@ -930,7 +952,7 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
         e.N = static_cast<int32_t>(p.n);
         e.K = static_cast<int32_t>(p.k);
         e.tiles_m = static_cast<int32_t>((p.m + s.macro_tile0 - 1) / s.macro_tile0);
-        e.tiles_n = static_cast<int32_t>((p.n + kTcTileN - 1) / kTcTileN);
+        e.tiles_n = static_cast<int32_t>((p.n + s.macro_tile1 - 1) / s.macro_tile1);
         e.alpha = p.alpha * scale_of(p.scale_a) * scale_of(p.scale_b);
         e.beta = p.beta;
         prefix[i + 1] = prefix[i] + static_cast<int64_t>(e.tiles_m) * e.tiles_n;
@@ -963,6 +985,7 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
     G.bm = s.macro_tile0;
     G.stages = s.stages;
     G.ctas = s.ctas;
+    G.cg = s.macro_tile1 / kTcTileN;
     G.err = h->d_err;
     G.timeout_ns = h->timeout_ns;
     G.sm_count = h->sm_count;
@@ -1026,14 +1049,15 @@ TL_API tl_status tl_tune_grouped(tl_handle* h, const tl_gemm_problem* probs, int
     cudaEventCreate(&e1);
     float best_t = 1e30f;
     bool any = false;
+    for (int cg : {1, 2})
     for (int bm : {64, 128, 192, 256}) {
         for (int stages : {3, 4, 6, 8}) {
             tl_gemm_solution c;
             memset(&c, 0, sizeof(c));
             c.kernel = TL_KERNEL_TCGEN05;
             c.macro_tile0 = bm;
-            c.macro_tile1 = kTcTileN;
-            c.stages = std::min(stages, max_stages(bm, h->smem_optin));
+            c.macro_tile1 = kTcTileN * cg;
+            c.stages = std::min(stages, max_stages(bm / cg, h->smem_optin));
             c.split_k = 1;
             if (stages > c.stages) continue;
             tl_grouped_plan* pl = nullptr;

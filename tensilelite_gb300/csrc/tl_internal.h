@@ -81,6 +81,7 @@ struct TcLaunch {
     int raster;
     int ctas;
     int promote_k;           // k elements per TMEM accumulation chain of the A0*B0 product (0: whole k)
+    int cg;                  // 1: one CTA per 128-row tile; 2: a CTA pair per 256-row tile
     // runtime
     int* err;
     uint64_t timeout_ns;
@@ -89,7 +90,8 @@ struct TcLaunch {
     int sm_count;
 };
 
-size_t tc_smem_bytes(int bm, int stages);
+// Dynamic shared memory of one CTA staging bm_cta m-rows per stage (bm / 2 for a CTA pair).
+size_t tc_smem_bytes(int bm_cta, int stages);
 int tc_tmem_cols(int bm);
 tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launches);
 // Checks a tcgen05 GEMM and fills its launch description without allocating anything; the caller
@@ -107,6 +109,7 @@ struct TcGroupLaunch {
     int count;
     int64_t total_tiles;
     int bm, stages, ctas;
+    int cg;                          // 1 or 2 (CTA pair)
     int* err;
     uint64_t timeout_ns;
     int sm_count;

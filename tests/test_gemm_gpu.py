@@ -150,6 +150,47 @@ def test_tc_solutions(h, bm, stages, split):
     check_case(h, case, "bf16", kernel="tcgen05", solution=sol)
 
 
+@pytest.mark.parametrize("dt", ["bf16", "fp16", "fp8"])
+@pytest.mark.parametrize("lay", ["TN", "NN", "NT", "TT"])
+@pytest.mark.parametrize("bm,split", [(256, 1), (128, 1), (256, 3)])
+def test_tc_cta_pair(h, dt, lay, bm, split):
+    """macro_tile1 = 256: a cluster of two CTAs per 256-row tile (tcgen05 cta_group::2)."""
+    if dt == "fp8" and lay[0] == "N" and bm == 128:
+        pytest.skip("MN-major fp8 A needs 128 m rows per CTA")
+    m, n, k = 520, 600, 704
+    case = gg.make_case(dt, lay, 300 + bm + split, m, n, k, ld_align=16)
+    sol = tl.Solution(kernel=tl.KERNEL_TCGEN05, macro_tile0=bm, macro_tile1=256,
+                      depth_u=128 if dt == "fp8" else 64, stages=4, split_k=split)
+    check_case(h, case, dt, kernel="tcgen05", solution=sol)
+
+
+def test_tc_cta_pair_promoted_bf16x6(h):
+    """The FP32-accurate path on a CTA pair with promotion (bm 128)."""
+    import torch
+    M, N, K = 512, 640, 2048
+    g = orc.rng(9)
+    A = orc.uniform_pm1(g, M * K).astype(np.float32)
+    B = orc.uniform_pm1(g, K * N).astype(np.float32)
+    dA, dB = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+    D = torch.empty(M * N, dtype=torch.float32, device="cuda")
+    sol = tl.Solution(kernel=tl.KERNEL_BF16X6, macro_tile0=128, macro_tile1=256, depth_u=64, stages=4,
+                      split_k=1, promote_k=256)
+    h.gemm(tl.Problem.make(M, N, K, dtype="fp32", kernel="bf16x6"), D, None, dA, dB, solution=sol)
+    ref = A.reshape(K, M).T.astype(np.float64) @ B.reshape(N, K).T.astype(np.float64)
+    got = D.cpu().numpy().reshape(N, M).T
+    assert orc.normwise_error(got, ref) < 1e-6
+
+
+def test_grouped_cta_pair(h):
+    probs, cases, D, C, A, B = _grouped_setup(16, 13)
+    sol = tl.Solution(kernel=tl.KERNEL_TCGEN05, macro_tile0=256, macro_tile1=256, depth_u=64, stages=6)
+    plan = h.grouped_plan(probs, D, C, A, B, solution=sol)
+    plan.launch()
+    h.device_status()
+    _check_grouped(cases, D)
+    plan.close()
+
+
 def test_tc_fp32_output_and_truncation(h):
     case = gg.make_case("bf16", "TN", 5, 200, 160, 512)
     got = gu.run_case(h, case, kernel="tcgen05", dtype="bf16", out_dtype="fp32")
