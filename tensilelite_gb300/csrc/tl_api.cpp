@@ -925,6 +925,7 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
         s.raster = 0;
     }
     s.kernel = TL_KERNEL_TCGEN05;
+    if (s.split_k == 0) s.split_k = 1;
     if (s.split_k != 1) return fail(TL_ERR_UNSUPPORTED, "grouped GEMM does not split k");
     for (int i = 0; i < count; ++i)
         if ((st = check_tc_solution(h, probs[i], s)) != TL_SUCCESS) return st;
