@@ -337,8 +337,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
     // CG == 2: a cluster of two CTAs on two SMs works on one 256-row tile.  Each CTA stages its own
     // 128 rows of the n-side operand and its half of the m-side operand; the leader (rank 0) issues
     // the pair MMAs, whose accumulator rows 0-127 live in the leader's TMEM and 128-255 in the peer's.
-    // TMA completions of both CTAs land on the leader's full barriers, MMA completions are multicast
-    // to both CTAs, and both epilogues release the leader's TMEM buffers with remote arrivals.
+    // The leader arms its full barriers with both CTAs' bytes and both CTAs' TMA completions land on
+    // them; MMA completions are multicast to both CTAs, and both epilogues release the leader's TMEM
+    // buffers with remote arrivals.
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const uint32_t bmc = static_cast<uint32_t>(p.bm) / CG;            // m-side rows staged by this CTA
@@ -369,7 +370,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < p.stages; ++s) {
-            ptx::mbar_init(&full[s], CG);
+            ptx::mbar_init(&full[s], 1);
             ptx::mbar_init(&empty[s], 1);
         }
         for (int a = 0; a < 2; ++a) {
@@ -431,8 +432,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         const void* mapM = p.group ? j.tmM : static_cast<const void*>(&p.tmM[p.term_m[v]]);
                         const int k0 = kb * W;
                         if constexpr (CG == 2) {
+                            // the leader arms its full barrier with both CTAs' bytes; the peer's loads
+                            // only complete transactions on it (they cannot run a phase ahead: the
+                            // peer refills a slot only after the leader's MMAs released it)
                             const uint32_t fb = ptx::mapa_shared(ptx::smem_u32(&full[stage]), 0);
-                            ptx::mbar_arrive_expect_tx_cluster(fb, stage_bytes);
+                            if (leader) ptx::mbar_arrive_expect_tx(&full[stage], 2u * stage_bytes);
                             if (!p.n_mn_major) {
                                 ptx::tma_load_3d_pair(sN, mapN, fb, k0, n0, j.b);
                             } else {
