@@ -409,65 +409,79 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
 
     if (warp == 0) {
         // ------------------------------------------------------------------ TMA producer (each CTA)
+        // One flat loop over (k-block, product) per tile; the bounded waits are single PTX blocks,
+        // so this single-lane loop has no data-dependent inner loop.
         if (lane == 0) {
             uint32_t stage = 0, phase = 0;
-            const int W = kTcRowBytes / (KIND == 0 ? 2 : 1);   // elements per 128-byte row
+            constexpr int W = kTcRowBytes / (KIND == 0 ? 2 : 1);   // elements per 128-byte row
+            const int n_mn = p.n_mn_major, m_mn = p.m_mn_major;
+            const int nstages = p.stages;
             bool ok = true;
             for (int64_t w = unit0; w < p.total_work && ok; w += units) {
                 TileJob j;
                 get_job(p, w, j);
                 const int n0 = j.n0 + static_cast<int>(rank) * kTcTileN;
                 const int m0 = j.m0 + static_cast<int>(rank * bmc);
-                for (int kb = j.kb0; kb < j.kb1 && ok; ++kb) {
-                    for (int v = 0; v < nvirt; ++v) {
-                        if (!ptx::mbar_wait(&empty[stage], phase ^ 1u, tlim, abort_flag)) {
-                            record_error(p, abort_flag, 1);
-                            ok = false;
-                            break;
-                        }
-                        uint8_t* sN = smem + static_cast<size_t>(stage) * stage_bytes;
-                        uint8_t* sM = sN + tileN_bytes;
-                        // split-precision products, smallest first (term table set by the host)
-                        const void* mapN = p.group ? j.tmN : static_cast<const void*>(&p.tmN[p.term_n[v]]);
-                        const void* mapM = p.group ? j.tmM : static_cast<const void*>(&p.tmM[p.term_m[v]]);
-                        const int k0 = kb * W;
-                        if constexpr (CG == 2) {
-                            // the leader arms its full barrier with both CTAs' bytes; the peer's loads
-                            // only complete transactions on it (they cannot run a phase ahead: the
-                            // peer refills a slot only after the leader's MMAs released it)
-                            const uint32_t fb = ptx::mapa_shared(ptx::smem_u32(&full[stage]), 0);
-                            if (leader) ptx::mbar_arrive_expect_tx(&full[stage], 2u * stage_bytes);
-                            if (!p.n_mn_major) {
-                                ptx::tma_load_3d_pair(sN, mapN, fb, k0, n0, j.b);
-                            } else {
-                                for (int c = 0; c < kTcTileN / W; ++c)
-                                    ptx::tma_load_3d_pair(sN + c * W * kTcRowBytes, mapN, fb, n0 + c * W, k0, j.b);
-                            }
-                            if (!p.m_mn_major) {
-                                ptx::tma_load_3d_pair(sM, mapM, fb, k0, m0, j.b);
-                            } else {
-                                for (int c = 0; c < static_cast<int>(bmc) / W; ++c)
-                                    ptx::tma_load_3d_pair(sM + c * W * kTcRowBytes, mapM, fb, m0 + c * W, k0, j.b);
-                            }
+                const int total = (j.kb1 - j.kb0) * nvirt;
+                int kb = j.kb0, v = 0;
+                for (int i = 0; i < total; ++i) {
+                    if (!ptx::mbar_wait(&empty[stage], phase ^ 1u, tlim)) {
+                        record_error(p, abort_flag, 1);
+                        ok = false;
+                        break;
+                    }
+                    uint8_t* sN = smem + static_cast<size_t>(stage) * stage_bytes;
+                    uint8_t* sM = sN + tileN_bytes;
+                    // split-precision products, smallest first (term table set by the host)
+                    const void* mapN = p.group ? j.tmN : static_cast<const void*>(&p.tmN[p.term_n[v]]);
+                    const void* mapM = p.group ? j.tmM : static_cast<const void*>(&p.tmM[p.term_m[v]]);
+                    const int k0 = kb * W;
+                    if constexpr (CG == 2) {
+                        // the leader arms its full barrier with both CTAs' bytes; the peer's loads
+                        // only complete transactions on it (they cannot run a phase ahead: the
+                        // peer refills a slot only after the leader's MMAs released it)
+                        const uint32_t fb = ptx::mapa_shared(ptx::smem_u32(&full[stage]), 0);
+                        if (leader) ptx::mbar_arrive_expect_tx(&full[stage], 2u * stage_bytes);
+                        if (!n_mn) {
+                            ptx::tma_load_3d_pair(sN, mapN, fb, k0, n0, j.b);
                         } else {
-                            ptx::mbar_arrive_expect_tx(&full[stage], stage_bytes);
-                            if (!p.n_mn_major) {
-                                ptx::tma_load_3d(sN, mapN, &full[stage], k0, n0, j.b);
-                            } else {
-                                for (int c = 0; c < kTcTileN / W; ++c)
-                                    ptx::tma_load_3d(sN + c * W * kTcRowBytes, mapN, &full[stage], n0 + c * W, k0, j.b);
-                            }
-                            if (!p.m_mn_major) {
-                                ptx::tma_load_3d(sM, mapM, &full[stage], k0, m0, j.b);
-                            } else {
-                                for (int c = 0; c < static_cast<int>(bmc) / W; ++c)
+#pragma unroll
+                            for (int c = 0; c < kTcTileN / W; ++c)
+                                ptx::tma_load_3d_pair(sN + c * W * kTcRowBytes, mapN, fb, n0 + c * W, k0, j.b);
+                        }
+                        if (!m_mn) {
+                            ptx::tma_load_3d_pair(sM, mapM, fb, k0, m0, j.b);
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < 4; ++c)      // bmc / W <= 4 chunks
+                                if (c * W < static_cast<int>(bmc))
+                                    ptx::tma_load_3d_pair(sM + c * W * kTcRowBytes, mapM, fb, m0 + c * W, k0, j.b);
+                        }
+                    } else {
+                        ptx::mbar_arrive_expect_tx(&full[stage], stage_bytes);
+                        if (!n_mn) {
+                            ptx::tma_load_3d(sN, mapN, &full[stage], k0, n0, j.b);
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < kTcTileN / W; ++c)
+                                ptx::tma_load_3d(sN + c * W * kTcRowBytes, mapN, &full[stage], n0 + c * W, k0, j.b);
+                        }
+                        if (!m_mn) {
+                            ptx::tma_load_3d(sM, mapM, &full[stage], k0, m0, j.b);
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < 4; ++c)      // bmc / W <= 4 chunks
+                                if (c * W < static_cast<int>(bmc))
                                     ptx::tma_load_3d(sM + c * W * kTcRowBytes, mapM, &full[stage], m0 + c * W, k0, j.b);
-                            }
                         }
-                        if (++stage == static_cast<uint32_t>(p.stages)) {
-                            stage = 0;
-                            phase ^= 1u;
-                        }
+                    }
+                    if (++stage == static_cast<uint32_t>(nstages)) {
+                        stage = 0;
+                        phase ^= 1u;
+                    }
+                    if (++v == nvirt) {
+                        v = 0;
+                        ++kb;
                     }
                 }
             }
@@ -478,9 +492,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
         // alternate between tiles).  With promotion the A0*B0 product restarts its accumulation
         // every promote_kb k-blocks in the alternate buffer (the epilogue drains each chain into
         // fp32 registers), and the small split-precision products accumulate for the whole tile in
-        // a separate pair of buffers.
+        // a separate pair of buffers.  One flat loop per tile over (k-block, product).
         if (lane == 0 && leader) {
             uint32_t stage = 0, phase = 0, mbuf = 0, mph = 0, sbuf = 0, sph = 0;
+            const uint32_t idesc = p.idesc;
+            const uint32_t n_kstep = p.n_kstep, m_kstep = p.m_kstep, n_lbo = p.n_lbo, m_lbo = p.m_lbo;
+            const uint32_t bmu = static_cast<uint32_t>(p.bm);
+            const int nstages = p.stages;
             bool ok = true;
             for (int64_t w = unit0; w < p.total_work && ok; w += units) {
                 TileJob j;
@@ -488,66 +506,82 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 const int nkb = j.kb1 - j.kb0;
                 const int chunk = promo ? p.promote_kb : (nkb > 0 ? nkb : 1);
                 if (sep_small) {
-                    if (!ptx::mbar_wait(&sempty[sbuf], sph ^ 1u, tlim, abort_flag)) {
+                    if (!ptx::mbar_wait(&sempty[sbuf], sph ^ 1u, tlim)) {
                         record_error(p, abort_flag, 2);
                         break;
                     }
                     ptx::tc_fence_after();
                 }
-                bool small_started = false;
-                for (int c0 = 0; c0 < nkb && ok; c0 += chunk) {
-                    if (!ptx::mbar_wait(&tempty[mbuf], mph ^ 1u, tlim, abort_flag)) {
+                if (nkb > 0) {
+                    if (!ptx::mbar_wait(&tempty[mbuf], mph ^ 1u, tlim)) {
                         record_error(p, abort_flag, 2);
+                        break;
+                    }
+                    ptx::tc_fence_after();
+                }
+                bool main_started = false, small_started = false;
+                const int total = nkb * nvirt;
+                int v = 0, kb_in_chain = 0;
+                for (int i = 0; i < total; ++i) {
+                    if (!ptx::mbar_wait(&full[stage], phase, tlim)) {
+                        record_error(p, abort_flag, 4);
                         ok = false;
                         break;
                     }
                     ptx::tc_fence_after();
-                    bool main_started = false;
-                    const int c1 = (c0 + chunk < nkb) ? c0 + chunk : nkb;
-                    for (int kb = c0; kb < c1 && ok; ++kb) {
-                        for (int v = 0; v < nvirt; ++v) {
-                            if (!ptx::mbar_wait(&full[stage], phase, tlim, abort_flag)) {
-                                record_error(p, abort_flag, 4);
+                    const bool is_main = !sep_small || v == nvirt - 1;
+                    const uint32_t d_tmem = tmem_base + (is_main ? mbuf * bmu : (2u + sbuf) * bmu);
+                    const bool started = is_main ? main_started : small_started;
+                    const uint32_t sN = ptx::smem_u32(smem + static_cast<size_t>(stage) * stage_bytes);
+                    const uint32_t sM = sN + tileN_bytes;
+#pragma unroll
+                    for (int ks = 0; ks < 4; ++ks) {
+                        const uint64_t adesc = ptx::sdesc_sw128(sN + ks * n_kstep, n_lbo, 1024);
+                        const uint64_t bdesc = ptx::sdesc_sw128(sM + ks * m_kstep, m_lbo, 1024);
+                        const uint32_t accumulate = (started || ks > 0) ? 1u : 0u;
+                        if constexpr (CG == 2) {
+                            if (KIND == 0) ptx::mma_f16_pair(d_tmem, adesc, bdesc, idesc, accumulate);
+                            else ptx::mma_f8_pair(d_tmem, adesc, bdesc, idesc, accumulate);
+                        } else {
+                            if (KIND == 0) ptx::mma_f16(d_tmem, adesc, bdesc, idesc, accumulate);
+                            else ptx::mma_f8(d_tmem, adesc, bdesc, idesc, accumulate);
+                        }
+                    }
+                    main_started = main_started || is_main;
+                    small_started = small_started || !is_main;
+                    if constexpr (CG == 2) ptx::mma_commit_pair(&empty[stage], 0x3);
+                    else ptx::mma_commit(&empty[stage]);
+                    if (++stage == static_cast<uint32_t>(nstages)) {
+                        stage = 0;
+                        phase ^= 1u;
+                    }
+                    if (++v == nvirt) {
+                        v = 0;
+                        // end of a chain of the main product: hand it to the epilogue, continue in
+                        // the other buffer (a tile's last chain is handed over after the loop)
+                        if (++kb_in_chain == chunk && i + 1 < total) {
+                            if constexpr (CG == 2) ptx::mma_commit_pair(&tfull[mbuf], 0x3);
+                            else ptx::mma_commit(&tfull[mbuf]);
+                            mbuf ^= 1u;
+                            if (mbuf == 0) mph ^= 1u;
+                            kb_in_chain = 0;
+                            main_started = false;
+                            if (!ptx::mbar_wait(&tempty[mbuf], mph ^ 1u, tlim)) {
+                                record_error(p, abort_flag, 2);
                                 ok = false;
                                 break;
                             }
                             ptx::tc_fence_after();
-                            const bool is_main = !sep_small || v == nvirt - 1;
-                            const uint32_t d_tmem = tmem_base + (is_main ? mbuf * static_cast<uint32_t>(p.bm)
-                                                                         : (2u + sbuf) * static_cast<uint32_t>(p.bm));
-                            const bool started = is_main ? main_started : small_started;
-                            const uint32_t sN = ptx::smem_u32(smem + static_cast<size_t>(stage) * stage_bytes);
-                            const uint32_t sM = sN + tileN_bytes;
-#pragma unroll
-                            for (int ks = 0; ks < 4; ++ks) {
-                                const uint64_t adesc = ptx::sdesc_sw128(sN + ks * p.n_kstep, p.n_lbo, 1024);
-                                const uint64_t bdesc = ptx::sdesc_sw128(sM + ks * p.m_kstep, p.m_lbo, 1024);
-                                const uint32_t accumulate = (started || ks > 0) ? 1u : 0u;
-                                if constexpr (CG == 2) {
-                                    if (KIND == 0) ptx::mma_f16_pair(d_tmem, adesc, bdesc, p.idesc, accumulate);
-                                    else ptx::mma_f8_pair(d_tmem, adesc, bdesc, p.idesc, accumulate);
-                                } else {
-                                    if (KIND == 0) ptx::mma_f16(d_tmem, adesc, bdesc, p.idesc, accumulate);
-                                    else ptx::mma_f8(d_tmem, adesc, bdesc, p.idesc, accumulate);
-                                }
-                            }
-                            if (is_main) main_started = true;
-                            else small_started = true;
-                            if constexpr (CG == 2) ptx::mma_commit_pair(&empty[stage], 0x3);
-                            else ptx::mma_commit(&empty[stage]);
-                            if (++stage == static_cast<uint32_t>(p.stages)) {
-                                stage = 0;
-                                phase ^= 1u;
-                            }
                         }
                     }
-                    if (!ok) break;
+                }
+                if (!ok) break;
+                if (nkb > 0) {
                     if constexpr (CG == 2) ptx::mma_commit_pair(&tfull[mbuf], 0x3);
                     else ptx::mma_commit(&tfull[mbuf]);
                     mbuf ^= 1u;
                     if (mbuf == 0) mph ^= 1u;
                 }
-                if (!ok) break;
                 if (sep_small) {
                     if constexpr (CG == 2) ptx::mma_commit_pair(&sfull[sbuf], 0x3);
                     else ptx::mma_commit(&sfull[sbuf]);

@@ -60,20 +60,36 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait on the phase with the given parity.  Returns false once `limit_ns` of wall time
-// has passed (the caller records the timeout and leaves its loop) or when *abort becomes non-zero
-// after the first millisecond of waiting.
+// Bounded wait on the phase with the given parity: spins on mbarrier.try_wait until the phase has
+// completed (true) or `limit_ns` of %globaltimer time has passed (false; the caller records the
+// timeout and leaves its loop).  The whole spin is one PTX block, so a single-lane issue loop that
+// calls it carries no data-dependent inner loop of its own (which measurably slowed tcgen05.mma
+// issue from such a loop).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns,
-                                          const volatile int* abort)
+                                          const volatile int* /*abort*/ = nullptr)
 {
-    if (mbar_try_wait(bar, parity)) return true;
-    const uint64_t t0 = globaltimer();
-    while (true) {
-        if (mbar_try_wait(bar, parity)) return true;
-        const uint64_t dt = globaltimer() - t0;
-        if (dt > limit_ns) return false;
-        if (dt > 1000000ull && *abort) return false;
-    }
+    uint32_t ok;
+    asm volatile(
+        "{\n\t"
+        ".reg .pred p, q;\n\t"
+        ".reg .u64 t0, t1;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "@p bra.uni TL_WAIT_DONE;\n\t"
+        "mov.u64 t0, %%globaltimer;\n\t"
+        "TL_WAIT_LOOP:\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "@p bra.uni TL_WAIT_DONE;\n\t"
+        "mov.u64 t1, %%globaltimer;\n\t"
+        "sub.u64 t1, t1, t0;\n\t"
+        "setp.lt.u64 q, t1, %3;\n\t"
+        "@q bra.uni TL_WAIT_LOOP;\n\t"
+        "TL_WAIT_DONE:\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t"
+        "}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "l"(limit_ns)
+        : "memory");
+    return ok != 0;
 }
 
 // ---- TMA ---------------------------------------------------------------------------------------
