@@ -98,7 +98,8 @@ class Solution(ctypes.Structure):
     _fields_ = [("kernel", ctypes.c_int32), ("macro_tile0", ctypes.c_int32), ("macro_tile1", ctypes.c_int32),
                 ("depth_u", ctypes.c_int32), ("stages", ctypes.c_int32), ("wave_tile0", ctypes.c_int32),
                 ("wave_tile1", ctypes.c_int32), ("split_k", ctypes.c_int32), ("raster", ctypes.c_int32),
-                ("ctas", ctypes.c_int32), ("promote_k", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+                ("ctas", ctypes.c_int32), ("promote_k", ctypes.c_int32),
+                ("tail_split", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}

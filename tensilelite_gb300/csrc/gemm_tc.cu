@@ -56,6 +56,8 @@ struct TcKernelParams {
                                   // k-blocks; the epilogue adds each chain into fp32 registers
     int tiles_m, tiles_n;
     int64_t total_work;
+    int64_t tail_start;           // work units below this are whole tiles; the rest split k
+    int tail_split;               // k splits of each tile from tail_start on
     int num_kb;
     int kb_elems;          // k elements per k-block (one 128-byte row)
     uint32_t idesc;
@@ -78,15 +80,26 @@ struct TileJob {
     float alpha, beta;
     int b, n0, m0;
     int kb0, kb1;
-    int split;
+    int split, nsplit;            // this unit's k split and the tile's number of splits
     int64_t tile;
+    int64_t slot;                 // split tiles: index of the tile's workspace slabs and counter
 };
 
 __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, TileJob& j)
 {
     if (p.group == nullptr) {
-        const int64_t tile = w / p.split_k;
-        const int split = static_cast<int>(w % p.split_k);
+        int64_t tile;
+        int split, nsplit;
+        if (w < p.tail_start) {
+            tile = w;
+            split = 0;
+            nsplit = 1;
+        } else {
+            const int64_t u = w - p.tail_start;
+            tile = p.tail_start + u / p.tail_split;
+            split = static_cast<int>(u % p.tail_split);
+            nsplit = p.tail_split;
+        }
         const int64_t tpb = static_cast<int64_t>(p.tiles_m) * p.tiles_n;
         const int b = static_cast<int>(tile / tpb);
         const int64_t t = tile % tpb;
@@ -116,10 +129,12 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, Tile
         j.b = b;
         j.n0 = in * p.tile_rows;
         j.m0 = jm * p.bm;
-        j.kb0 = static_cast<int>((static_cast<int64_t>(split) * p.num_kb) / p.split_k);
-        j.kb1 = static_cast<int>((static_cast<int64_t>(split + 1) * p.num_kb) / p.split_k);
+        j.kb0 = static_cast<int>((static_cast<int64_t>(split) * p.num_kb) / nsplit);
+        j.kb1 = static_cast<int>((static_cast<int64_t>(split + 1) * p.num_kb) / nsplit);
         j.split = split;
+        j.nsplit = nsplit;
         j.tile = tile;
+        j.slot = tile - p.tail_start;
     } else {
         // binary search: group_prefix[g] <= w < group_prefix[g+1]
         int lo = 0, hi = p.group_count - 1;
@@ -147,7 +162,9 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, Tile
         j.kb0 = 0;
         j.kb1 = (e.K + p.kb_elems - 1) / p.kb_elems;
         j.split = 0;
+        j.nsplit = 1;
         j.tile = w;
+        j.slot = 0;
     }
 }
 
@@ -285,7 +302,7 @@ __device__ __forceinline__ void split_finish(const TcKernelParams& p, const Tile
     asm volatile("bar.sync 1, 128;" ::: "memory");
     if (et == 0) {
         int last = 0;
-        if (ok) last = (atomicAdd(p.counters + j.tile, 1) == p.split_k - 1) ? 1 : 0;
+        if (ok) last = (atomicAdd(p.counters + j.slot, 1) == j.nsplit - 1) ? 1 : 0;
         *last_flag = last;
     }
     asm volatile("bar.sync 1, 128;" ::: "memory");
@@ -297,9 +314,9 @@ __device__ __forceinline__ void split_finish(const TcKernelParams& p, const Tile
             float v[32];
 #pragma unroll
             for (int i = 0; i < 32; ++i) v[i] = 0.f;
-            for (int s = 0; s < p.split_k; ++s) {
+            for (int s = 0; s < j.nsplit; ++s) {
                 const float4* src = reinterpret_cast<const float4*>(
-                    p.ws + (static_cast<size_t>(j.tile) * p.split_k + s) * (static_cast<size_t>(kTcTileN) * p.bm) +
+                    p.ws + (static_cast<size_t>(j.slot) * j.nsplit + s) * (static_cast<size_t>(kTcTileN) * p.bm) +
                     (static_cast<size_t>(c) * kTcTileN + row) * 32);
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
@@ -313,7 +330,7 @@ __device__ __forceinline__ void split_finish(const TcKernelParams& p, const Tile
             const int m = j.m0 + c * 32;
             if (row_ok && m < j.M) store_chunk<TD>(j, base_c, base_d, m, v, p.out_trunc);
         }
-        if (et == 0) p.counters[j.tile] = 0;   // ready for the next launch
+        if (et == 0) p.counters[j.slot] = 0;   // ready for the next launch
     }
     asm volatile("bar.sync 1, 128;" ::: "memory");   // last_flag is reused by the next tile
 }
@@ -606,7 +623,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             TileJob j;
             get_job(p, w, j);
             j.n0 += static_cast<int>(rank) * kTcTileN;
-            j.tile = j.tile * CG + rank;              // split-k slabs and counters per CTA half
+            j.slot = j.slot * CG + rank;              // split-k slabs and counters per CTA half
             const int n = j.n0 + row;
             const bool row_ok = n < j.N;
             const int64_t base_d = static_cast<int64_t>(j.b) * p.stride_d + static_cast<int64_t>(n) * j.ldd;
@@ -664,7 +681,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                     sbuf ^= 1u;
                     if (sbuf == 0) sph ^= 1u;
                 }
-                if (p.split_k == 1) {
+                if (j.nsplit == 1) {
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
                         const int m = j.m0 + q * 32;
@@ -676,7 +693,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         }
                     }
                 } else {
-                    float* slab = p.ws + (static_cast<size_t>(j.tile) * p.split_k + j.split) *
+                    float* slab = p.ws + (static_cast<size_t>(j.slot) * j.nsplit + j.split) *
                                              (static_cast<size_t>(kTcTileN) * p.bm);
                     if (ok) {
 #pragma unroll
@@ -701,7 +718,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             }
             const uint32_t tbase = tmem_base + lane_off + mbuf * static_cast<uint32_t>(p.bm);
             if (ok) ptx::tc_fence_after();
-            if (p.split_k == 1) {
+            if (j.nsplit == 1) {
                 for (int c = 0; c < chunks && ok; ++c) {
                     uint32_t r[32];
                     __syncwarp();
@@ -717,7 +734,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 }
             } else {
                 // split-k: park this split's partial tile, thread-private layout [chunk][row][32]
-                float* slab = p.ws + (static_cast<size_t>(j.tile) * p.split_k + j.split) *
+                float* slab = p.ws + (static_cast<size_t>(j.slot) * j.nsplit + j.split) *
                                          (static_cast<size_t>(kTcTileN) * p.bm);
                 for (int c = 0; c < chunks && ok; ++c) {
                     uint32_t r[32];
@@ -849,33 +866,33 @@ tl_status dispatch_cg(int in_dtype, int out_dtype, const TcKernelParams& kp, int
     return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel: unsupported output type");
 }
 
+// Persistent workers of a launch: CTAs (CG 1) or co-resident CTA pairs (CG 2).
+int persistent_workers(int in_dtype, int out_dtype, int cg, int ctas, int sm_count, size_t smem)
+{
+    if (cg == 1) return ctas > 0 ? ctas : sm_count;
+    if (ctas > 0) return ctas / 2 > 0 ? ctas / 2 : 1;
+    const int kind = (in_dtype == TL_DTYPE_FP8_E4M3) ? 1 : 0;
+    int maxc = 0;
+    if (kind == 0)
+        maxc = out_dtype == TL_DTYPE_FP32   ? max_pair_clusters<0, float>(smem)
+               : out_dtype == TL_DTYPE_FP16 ? max_pair_clusters<0, __half>(smem)
+                                            : max_pair_clusters<0, __nv_bfloat16>(smem);
+    else
+        maxc = out_dtype == TL_DTYPE_FP32   ? max_pair_clusters<1, float>(smem)
+               : out_dtype == TL_DTYPE_FP16 ? max_pair_clusters<1, __half>(smem)
+                                            : max_pair_clusters<1, __nv_bfloat16>(smem);
+    return maxc > 0 ? maxc : sm_count / 2;
+}
+
 // Grid: one CTA per SM (CG 1) or as many co-resident pairs as fit (CG 2), never more than the work.
 tl_status dispatch(int in_dtype, int out_dtype, int cg, const TcKernelParams& kp, int ctas, int sm_count,
                    int64_t total_work, size_t smem, cudaStream_t s)
 {
-    if (cg == 1) {
-        int grid = ctas > 0 ? ctas : sm_count;
-        if (grid > total_work) grid = static_cast<int>(total_work);
-        if (grid < 1) grid = 1;
-        return dispatch_cg<1>(in_dtype, out_dtype, kp, grid, smem, s);
-    }
-    int pairs = ctas > 0 ? ctas / 2 : 0;
-    if (pairs <= 0) {
-        const int kind = (in_dtype == TL_DTYPE_FP8_E4M3) ? 1 : 0;
-        int maxc = 0;
-        if (kind == 0)
-            maxc = out_dtype == TL_DTYPE_FP32   ? max_pair_clusters<0, float>(smem)
-                   : out_dtype == TL_DTYPE_FP16 ? max_pair_clusters<0, __half>(smem)
-                                                : max_pair_clusters<0, __nv_bfloat16>(smem);
-        else
-            maxc = out_dtype == TL_DTYPE_FP32   ? max_pair_clusters<1, float>(smem)
-                   : out_dtype == TL_DTYPE_FP16 ? max_pair_clusters<1, __half>(smem)
-                                                : max_pair_clusters<1, __nv_bfloat16>(smem);
-        pairs = maxc > 0 ? maxc : sm_count / 2;
-    }
-    if (pairs > total_work) pairs = static_cast<int>(total_work);
-    if (pairs < 1) pairs = 1;
-    return dispatch_cg<2>(in_dtype, out_dtype, kp, 2 * pairs, smem, s);
+    int workers = persistent_workers(in_dtype, out_dtype, cg, ctas, sm_count, smem);
+    if (workers > total_work) workers = static_cast<int>(total_work);
+    if (workers < 1) workers = 1;
+    if (cg == 1) return dispatch_cg<1>(in_dtype, out_dtype, kp, workers, smem, s);
+    return dispatch_cg<2>(in_dtype, out_dtype, kp, 2 * workers, smem, s);
 }
 
 uint32_t make_idesc(int in_dtype, int n_mn_major, int m_mn_major, int bm, int cg)
@@ -1003,7 +1020,34 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     kp.num_kb = static_cast<int>((L.K + W - 1) / W);
     kp.kb_elems = W;
     kp.promote_kb = L.promote_k > 0 ? static_cast<int>((L.promote_k + W - 1) / W) : 0;
-    kp.total_work = static_cast<int64_t>(kp.tiles_m) * kp.tiles_n * L.batch * L.split_k;
+    const size_t smem = tc_smem_bytes(L.bm / cg, L.stages);
+    const int64_t tiles = static_cast<int64_t>(kp.tiles_m) * kp.tiles_n * L.batch;
+    if (L.split_k > 1) {
+        kp.tail_start = 0;
+        kp.tail_split = L.split_k;
+        kp.total_work = tiles * L.split_k;
+    } else {
+        // tail split: when the last wave of whole tiles would leave at least half of the persistent
+        // workers idle, split that wave's tiles along k so it finishes in a fraction of a wave
+        kp.tail_start = tiles;
+        kp.tail_split = 1;
+        kp.total_work = tiles;
+        const int workers = persistent_workers(L.in_dtype, L.out_dtype, cg, L.ctas, L.sm_count, smem);
+        if (L.tail_split != 1 && L.workspace && tiles > workers) {
+            const int64_t rem = tiles % workers;
+            if (rem > 0 && 2 * rem <= workers) {
+                int S = L.tail_split > 1 ? L.tail_split : static_cast<int>(workers / rem);
+                if (S > kp.num_kb) S = kp.num_kb;
+                if (S > 8) S = 8;
+                const size_t need = static_cast<size_t>(rem) * cg * S * kTcTileN * L.bm * sizeof(float);
+                if (S >= 2 && static_cast<size_t>(rem) * cg <= L.counters_len && need <= L.workspace_bytes) {
+                    kp.tail_start = tiles - rem;
+                    kp.tail_split = S;
+                    kp.total_work = kp.tail_start + rem * S;
+                }
+            }
+        }
+    }
     kp.n_mn_major = L.opN[0].mn_major;
     kp.m_mn_major = L.opM[0].mn_major;
     kp.idesc = make_idesc(L.in_dtype, kp.n_mn_major, kp.m_mn_major, L.bm, cg);
@@ -1014,7 +1058,6 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     kp.counters = L.counters;
     kp.err = L.err;
     kp.timeout_ns = L.timeout_ns;
-    const size_t smem = tc_smem_bytes(L.bm / cg, L.stages);
     st = dispatch(L.in_dtype, L.out_dtype, cg, kp, L.ctas, L.sm_count, kp.total_work, smem, stream);
     if (st == TL_SUCCESS && launches) ++*launches;
     return st;
@@ -1032,6 +1075,8 @@ tl_status tc_grouped_launch(const TcGroupLaunch& G, cudaStream_t stream, int64_t
     kp.split_k = 1;
     kp.nterms = 1;
     kp.total_work = G.total_tiles;
+    kp.tail_start = G.total_tiles;
+    kp.tail_split = 1;
     kp.kb_elems = kTcRowBytes / dtype_bytes(G.in_dtype);
     kp.stride_c = 0;
     kp.stride_d = 0;

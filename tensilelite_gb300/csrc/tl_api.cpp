@@ -252,6 +252,7 @@ tl_status check_tc_solution(const tl_handle* h, const tl_gemm_problem& p, const 
         return fail(TL_ERR_UNSUPPORTED, "split_k must be in [1, min(64, k blocks)]");
     if (s.raster < 0 || s.ctas < 0) return fail(TL_ERR_INVALID_ARG, "raster and ctas must be >= 0");
     if (s.promote_k < 0) return fail(TL_ERR_INVALID_ARG, "promote_k must be >= 0");
+    if (s.tail_split < 0 || s.tail_split > 8) return fail(TL_ERR_INVALID_ARG, "tail_split must be in [0, 8]");
     if (s.promote_k > 0 && bm != 128)
         return fail(TL_ERR_UNSUPPORTED, "promote_k needs macro_tile0 == 128 (fp32 running sums, TMEM budget)");
     return TL_SUCCESS;
@@ -334,6 +335,7 @@ struct Prepared {
     uint16_t* b_pc[3] = {nullptr, nullptr, nullptr};
     int64_t a_span = 0, b_span = 0;
     float* ws_partials = nullptr;
+    size_t part_bytes = 0;
 };
 
 int64_t operand_span(int64_t ld, int64_t cols, int64_t batch, int64_t bstride, int64_t rows)
@@ -420,8 +422,16 @@ tl_status prepare(tl_handle* h, const tl_gemm_problem* prob, const tl_gemm_solut
                           ((p.m + P.s.macro_tile0 - 1) / P.s.macro_tile0) * p.batch;
     if (P.s.split_k > 1) {
         off_part = need;
-        need = off_part + static_cast<size_t>(tiles) * P.s.split_k * kTcTileN * P.s.macro_tile0 * sizeof(float);
+        P.part_bytes = static_cast<size_t>(tiles) * P.s.split_k * kTcTileN * P.s.macro_tile0 * sizeof(float);
+        need = off_part + P.part_bytes;
         if ((st = ensure_counters(h, static_cast<size_t>(tiles))) != TL_SUCCESS) return st;
+    } else if (P.s.tail_split != 1) {
+        // a split last wave uses at most one slab set per SM: split tiles x splits <= workers
+        off_part = need;
+        P.part_bytes = static_cast<size_t>(h->sm_count) * kTcTileN * P.s.macro_tile0 * sizeof(float) *
+                       static_cast<size_t>(P.s.tail_split > 1 ? P.s.tail_split : 1);
+        need = off_part + P.part_bytes;
+        if ((st = ensure_counters(h, static_cast<size_t>(h->sm_count))) != TL_SUCCESS) return st;
     }
     if (need) {
         if ((st = ensure_ws(h, need)) != TL_SUCCESS) return st;
@@ -432,7 +442,7 @@ tl_status prepare(tl_handle* h, const tl_gemm_problem* prob, const tl_gemm_solut
                 P.b_pc[i] = reinterpret_cast<uint16_t*>(base + off_b[i]);
             }
         }
-        if (P.s.split_k > 1) P.ws_partials = reinterpret_cast<float*>(base + off_part);
+        if (P.part_bytes) P.ws_partials = reinterpret_cast<float*>(base + off_part);
     }
     if (is_split(kernel)) {
         // the split copies keep the caller's leading dimensions; TMA needs them 16-byte aligned in bf16
@@ -502,7 +512,10 @@ tl_status enqueue(tl_handle* h, const Prepared& P, cudaStream_t s)
     L.err = h->d_err;
     L.timeout_ns = h->timeout_ns;
     L.workspace = P.ws_partials;
+    L.workspace_bytes = P.part_bytes;
     L.counters = h->counters;
+    L.counters_len = h->counters_len;
+    L.tail_split = P.s.tail_split;
     L.sm_count = h->sm_count;
     return tc_gemm_launch(L, s, &h->launches);
 }
@@ -556,7 +569,7 @@ std::vector<tl_gemm_solution> tc_candidates(const tl_handle* h, const tl_gemm_pr
 tl_status save_cache(const char* path, const std::string& key, const tl_gemm_solution& s, float ms)
 {
     // line-oriented JSON object:
-    //   "key": [kernel, mt0, mt1, du, stages, wt0, wt1, split, raster, ctas, promote_k, ms]
+    //   "key": [kernel, mt0, mt1, du, stages, wt0, wt1, split, raster, ctas, promote_k, tail_split, ms]
     std::map<std::string, std::string> lines;
     {
         std::ifstream in(path);
@@ -572,9 +585,9 @@ tl_status save_cache(const char* path, const std::string& key, const tl_gemm_sol
         }
     }
     char buf[256];
-    snprintf(buf, sizeof(buf), " [%d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %.6f]", s.kernel, s.macro_tile0,
+    snprintf(buf, sizeof(buf), " [%d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %.6f]", s.kernel, s.macro_tile0,
              s.macro_tile1, s.depth_u, s.stages, s.wave_tile0, s.wave_tile1, s.split_k, s.raster, s.ctas,
-             s.promote_k, ms);
+             s.promote_k, s.tail_split, ms);
     lines[key] = buf;
     std::ofstream out(path, std::ios::trunc);
     if (!out) return fail(TL_ERR_INVALID_ARG, std::string("cannot write ") + path);
@@ -644,6 +657,7 @@ tl_status plan_tc_noalloc(int sm_count, size_t smem_optin, const tl_gemm_problem
     L->ctas = s.ctas;
     L->promote_k = s.promote_k;
     L->cg = cgp;
+    L->tail_split = 1;     // the static scratch is sized for explicit split-k only
     L->sm_count = sm_count;
     return TL_SUCCESS;
 }
@@ -868,9 +882,9 @@ TL_API tl_status tl_load_solutions(tl_handle* h, const char* path, int* loaded)
         tl_gemm_solution s;
         memset(&s, 0, sizeof(s));
         float ms = 0;
-        if (sscanf(line.c_str() + b0, "[%d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %f", &s.kernel, &s.macro_tile0,
-                   &s.macro_tile1, &s.depth_u, &s.stages, &s.wave_tile0, &s.wave_tile1, &s.split_k, &s.raster, &s.ctas,
-                   &s.promote_k, &ms) == 12) {
+        if (sscanf(line.c_str() + b0, "[%d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %d, %f", &s.kernel,
+                   &s.macro_tile0, &s.macro_tile1, &s.depth_u, &s.stages, &s.wave_tile0, &s.wave_tile1, &s.split_k,
+                   &s.raster, &s.ctas, &s.promote_k, &s.tail_split, &ms) == 13) {
             std::lock_guard<std::mutex> g(h->mu);
             h->tuned[key] = s;
             ++n;

@@ -86,7 +86,10 @@ struct TcLaunch {
     int* err;
     uint64_t timeout_ns;
     float* workspace;        // split-k partials
+    size_t workspace_bytes;
     int* counters;           // split-k arrival counters (zeroed, self-resetting)
+    size_t counters_len;
+    int tail_split;          // 0 auto, 1 off, S: k splits of the last partial wave's tiles
     int sm_count;
 };
 

@@ -191,6 +191,19 @@ def test_grouped_cta_pair(h):
     plan.close()
 
 
+@pytest.mark.parametrize("cg,bm", [(1, 256), (2, 256), (1, 128)])
+def test_tail_split_last_wave(h, cg, bm):
+    """More tiles than persistent workers with a small remainder: the last wave's tiles are split
+    along k (auto tail_split) and reduced through the workspace."""
+    m, n, k = 1024, 5120, 1024
+    case = gg.make_case("bf16", "NN", 500 + cg + bm, m, n, k)
+    sol = tl.Solution(kernel=tl.KERNEL_TCGEN05, macro_tile0=bm, macro_tile1=128 * cg, depth_u=64,
+                      stages=4, split_k=1, tail_split=0)
+    check_case(h, case, "bf16", kernel="tcgen05", solution=sol)
+    sol.tail_split = 3
+    check_case(h, case, "bf16", kernel="tcgen05", solution=sol)
+
+
 def test_tc_fp32_output_and_truncation(h):
     case = gg.make_case("bf16", "TN", 5, 200, 160, 512)
     got = gu.run_case(h, case, kernel="tcgen05", dtype="bf16", out_dtype="fp32")
