@@ -290,7 +290,7 @@ __device__ __forceinline__ void store_chunk(const TileJob& j, int64_t base_c, in
 }
 
 // Split-k completion, run by the four epilogue warps after this split parked its partial tile in
-// the workspace: the last split of a tile to arrive (per-tile counter) sums every split's partial
+// the workspace (layout [32-column chunk][column][row], so every warp access is one 128-byte line): the last split of a tile to arrive (per-tile counter) sums every split's partial
 // in split order -- so the result does not depend on which CTA finished last -- and runs the
 // epilogue.  The counter is reset for the next launch.  Every thread passes the same three named
 // barriers whether or not it has work, so a warp that gave up on a wait cannot strand the others.
@@ -315,17 +315,10 @@ __device__ __forceinline__ void split_finish(const TcKernelParams& p, const Tile
 #pragma unroll
             for (int i = 0; i < 32; ++i) v[i] = 0.f;
             for (int s = 0; s < j.nsplit; ++s) {
-                const float4* src = reinterpret_cast<const float4*>(
-                    p.ws + (static_cast<size_t>(j.slot) * j.nsplit + s) * (static_cast<size_t>(kTcTileN) * p.bm) +
-                    (static_cast<size_t>(c) * kTcTileN + row) * 32);
+                const float* src = p.ws + (static_cast<size_t>(j.slot) * j.nsplit + s) * (static_cast<size_t>(kTcTileN) * p.bm) +
+                                   static_cast<size_t>(c) * 32 * kTcTileN + row;
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    const float4 f = __ldcg(src + q);
-                    v[4 * q] += f.x;
-                    v[4 * q + 1] += f.y;
-                    v[4 * q + 2] += f.z;
-                    v[4 * q + 3] += f.w;
-                }
+                for (int i = 0; i < 32; ++i) v[i] += __ldcg(src + i * kTcTileN);
             }
             const int m = j.m0 + c * 32;
             if (row_ok && m < j.M) store_chunk<TD>(j, base_c, base_d, m, v, p.out_trunc);
@@ -628,6 +621,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             const bool row_ok = n < j.N;
             const int64_t base_d = static_cast<int64_t>(j.b) * p.stride_d + static_cast<int64_t>(n) * j.ldd;
             const int64_t base_c = static_cast<int64_t>(j.b) * p.stride_c + static_cast<int64_t>(n) * j.ldc;
+            if (ok && row_ok && j.beta != 0.0f && j.C != nullptr && (j.nsplit == 1 || j.split == j.nsplit - 1)) {
+                // C does not depend on the accumulator: start pulling this row's segment into L2
+                // while the tile is still accumulating
+                const char* cp = static_cast<const char*>(j.C) + (base_c + j.m0) * static_cast<int64_t>(sizeof(TD));
+                const int cbytes = (min(p.bm, j.M - j.m0)) * static_cast<int>(sizeof(TD));
+                for (int off = 0; off < cbytes; off += 128)
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(cp + off));
+            }
             if (promo) {
                 // ---- promotion: sum the A0*B0 chains (and the small terms) in fp32 registers; bm == 128
                 float run[128];
@@ -698,11 +699,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                     if (ok) {
 #pragma unroll
                         for (int q = 0; q < 4; ++q) {
-                            float4* dst = reinterpret_cast<float4*>(slab + (static_cast<size_t>(q) * kTcTileN + row) * 32);
+                            float* dst = slab + static_cast<size_t>(q) * 32 * kTcTileN + row;
 #pragma unroll
-                            for (int e = 0; e < 8; ++e)
-                                __stcg(dst + e, make_float4(run[q * 32 + 4 * e], run[q * 32 + 4 * e + 1],
-                                                            run[q * 32 + 4 * e + 2], run[q * 32 + 4 * e + 3]));
+                            for (int i = 0; i < 32; ++i) __stcg(dst + i * kTcTileN, run[q * 32 + i]);
                         }
                     }
                     split_finish<TD>(p, j, ok, et, row, row_ok, base_c, base_d, last_flag);
@@ -733,7 +732,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                     }
                 }
             } else {
-                // split-k: park this split's partial tile, thread-private layout [chunk][row][32]
+                // split-k: park this split's partial tile, layout [chunk][column][row] (coalesced)
                 float* slab = p.ws + (static_cast<size_t>(j.slot) * j.nsplit + j.split) *
                                          (static_cast<size_t>(kTcTileN) * p.bm);
                 for (int c = 0; c < chunks && ok; ++c) {
@@ -741,11 +740,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                     __syncwarp();
                     ptx::tmem_ld32(tbase + c * 32, r);
                     if (c == chunks - 1) release_tmem<CG>(&tempty[mbuf], lane);
-                    float4* dst = reinterpret_cast<float4*>(slab + (static_cast<size_t>(c) * kTcTileN + row) * 32);
+                    float* dst = slab + static_cast<size_t>(c) * 32 * kTcTileN + row;
 #pragma unroll
-                    for (int q = 0; q < 8; ++q)
-                        __stcg(dst + q, make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
-                                                    __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3])));
+                    for (int i = 0; i < 32; ++i) __stcg(dst + i * kTcTileN, __uint_as_float(r[i]));
                 }
                 split_finish<TD>(p, j, ok, et, row, row_ok, base_c, base_d, last_flag);
             }
