@@ -314,11 +314,24 @@ __device__ __forceinline__ void split_finish(const TcKernelParams& p, const Tile
             float v[32];
 #pragma unroll
             for (int i = 0; i < 32; ++i) v[i] = 0.f;
-            for (int s = 0; s < j.nsplit; ++s) {
-                const float* src = p.ws + (static_cast<size_t>(j.slot) * j.nsplit + s) * (static_cast<size_t>(kTcTileN) * p.bm) +
-                                   static_cast<size_t>(c) * 32 * kTcTileN + row;
+            const size_t slab_elems = static_cast<size_t>(kTcTileN) * p.bm;
+            const float* src0 = p.ws + static_cast<size_t>(j.slot) * j.nsplit * slab_elems +
+                                static_cast<size_t>(c) * 32 * kTcTileN + row;
+            for (int s = 0; s < j.nsplit; s += 2) {       // two slabs' loads in flight per step
+                float a[32], b[32];
+                const float* sa = src0 + static_cast<size_t>(s) * slab_elems;
+                const bool two = s + 1 < j.nsplit;
 #pragma unroll
-                for (int i = 0; i < 32; ++i) v[i] += __ldcg(src + i * kTcTileN);
+                for (int i = 0; i < 32; ++i) {
+                    a[i] = __ldcg(sa + i * kTcTileN);
+                    b[i] = two ? __ldcg(sa + slab_elems + i * kTcTileN) : 0.f;
+                }
+#pragma unroll
+                for (int i = 0; i < 32; ++i) v[i] += a[i];
+                if (two) {
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) v[i] += b[i];
+                }
             }
             const int m = j.m0 + c * 32;
             if (row_ok && m < j.M) store_chunk<TD>(j, base_c, base_d, m, v, p.out_trunc);
@@ -339,6 +352,58 @@ __device__ __forceinline__ void release_tmem(uint64_t* bar, int lane)
         if constexpr (CG == 2) ptx::mbar_arrive_cluster(ptx::mapa_shared(ptx::smem_u32(bar), 0));
         else ptx::mbar_arrive(bar);
     }
+}
+
+// Split-k completion that keeps this split's own partial in TMEM: the partial was parked in the
+// workspace for the other splits; if this CTA is the last of the tile to arrive it sums the
+// partials in split order -- its own read back from TMEM, the others from the workspace with all of
+// a chunk's loads in flight -- and runs the epilogue.  The TMEM buffer is released afterwards.
+template <typename TD, int CG>
+__device__ __forceinline__ void split_finish_tmem(const TcKernelParams& p, const TileJob& j, bool ok, int et, int lane,
+                                                  int row, bool row_ok, int64_t base_c, int64_t base_d,
+                                                  volatile int* last_flag, uint32_t tbase, uint64_t* tempty_bar)
+{
+    __threadfence();
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    if (et == 0) {
+        int last = 0;
+        if (ok) last = (atomicAdd(p.counters + j.slot, 1) == j.nsplit - 1) ? 1 : 0;
+        *last_flag = last;
+    }
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    const int is_last = *last_flag;
+    if (is_last && ok) {
+        __threadfence();
+        const int chunks = p.bm / 32;
+        const size_t slab_elems = static_cast<size_t>(kTcTileN) * p.bm;
+        const float* base = p.ws + static_cast<size_t>(j.slot) * j.nsplit * slab_elems + row;
+        for (int c = 0; c < chunks; ++c) {
+            float v[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) v[i] = 0.f;
+            for (int s = 0; s < j.nsplit; ++s) {
+                if (s == j.split) {
+                    uint32_t r[32];
+                    __syncwarp();
+                    ptx::tmem_ld32(tbase + c * 32, r);
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) v[i] += __uint_as_float(r[i]);
+                } else {
+                    float a[32];
+                    const float* src = base + static_cast<size_t>(s) * slab_elems + static_cast<size_t>(c) * 32 * kTcTileN;
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) a[i] = __ldcg(src + i * kTcTileN);
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) v[i] += a[i];
+                }
+            }
+            const int m = j.m0 + c * 32;
+            if (row_ok && m < j.M) store_chunk<TD>(j, base_c, base_d, m, v, p.out_trunc);
+        }
+        if (et == 0) p.counters[j.slot] = 0;   // ready for the next launch
+    }
+    if (ok) release_tmem<CG>(tempty_bar, lane);
+    asm volatile("bar.sync 1, 128;" ::: "memory");   // last_flag is reused by the next tile
 }
 
 template <int KIND, typename TD, int CG>
@@ -739,12 +804,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                     uint32_t r[32];
                     __syncwarp();
                     ptx::tmem_ld32(tbase + c * 32, r);
-                    if (c == chunks - 1) release_tmem<CG>(&tempty[mbuf], lane);
                     float* dst = slab + static_cast<size_t>(c) * 32 * kTcTileN + row;
 #pragma unroll
                     for (int i = 0; i < 32; ++i) __stcg(dst + i * kTcTileN, __uint_as_float(r[i]));
                 }
-                split_finish<TD>(p, j, ok, et, row, row_ok, base_c, base_d, last_flag);
+                split_finish_tmem<TD, CG>(p, j, ok, et, lane, row, row_ok, base_c, base_d, last_flag, tbase,
+                                          &tempty[mbuf]);
             }
             mbuf ^= 1u;
             if (mbuf == 0) mph ^= 1u;
