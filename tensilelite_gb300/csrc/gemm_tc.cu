@@ -341,6 +341,84 @@ __device__ __forceinline__ void split_finish(const TcKernelParams& p, const Tile
     asm volatile("bar.sync 1, 128;" ::: "memory");   // last_flag is reused by the next tile
 }
 
+// C for one 32-output chunk, loaded ahead of its use (the epilogue keeps the next chunk's loads in
+// flight while it finishes the current one).  16-bit outputs occupy cw[0..15] as packed pairs.
+template <typename TD>
+__device__ __forceinline__ void load_c_chunk(const TileJob& j, int64_t base_c, int m, uint32_t (&cw)[32])
+{
+    if (!(j.beta != 0.0f && j.C != nullptr) || m >= j.M) return;
+    const char* cptr = static_cast<const char*>(j.C) + (base_c + m) * Out<TD>::kBytes;
+    if (m + 32 <= j.M && (reinterpret_cast<uintptr_t>(cptr) & 15) == 0) {
+        constexpr int nvec = sizeof(TD) == 4 ? 8 : 4;
+#pragma unroll
+        for (int q = 0; q < nvec; ++q) {
+            const uint4 w = __ldg(reinterpret_cast<const uint4*>(cptr) + q);
+            cw[4 * q] = w.x;
+            cw[4 * q + 1] = w.y;
+            cw[4 * q + 2] = w.z;
+            cw[4 * q + 3] = w.w;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+            const float c = (m + i < j.M) ? Out<TD>::load(j.C, base_c + m + i) : 0.f;
+            if constexpr (sizeof(TD) == 4) {
+                cw[i] = __float_as_uint(c);
+            } else {
+                // repack as the vector path does: element i in the low (even) / high (odd) half
+                const uint32_t bits = (sizeof(TD) == 2 && std::is_same<TD, __half>::value)
+                                          ? static_cast<uint32_t>(__half_as_ushort(__float2half_rn(c)))
+                                          : (__float_as_uint(c) >> 16);
+                if (i & 1) cw[i >> 1] |= bits << 16;
+                else cw[i >> 1] = bits;
+            }
+        }
+    }
+}
+
+// Finish a chunk with C already in registers (from load_c_chunk): v = alpha*acc + beta*C, store.
+template <typename TD>
+__device__ __forceinline__ void store_chunk_pre(const TileJob& j, int64_t base_d, int m, float (&acc)[32],
+                                                const uint32_t (&cw)[32], int trunc)
+{
+    const bool use_c = (j.beta != 0.0f) && (j.C != nullptr);
+    float c[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) {
+        if constexpr (sizeof(TD) == 4) {
+            c[i] = __uint_as_float(cw[i]);
+        } else {
+            const uint32_t w = cw[i >> 1];
+            float lo, hi;
+            unpack2(w, std::is_same<TD, __half>::value ? 1 : 0, lo, hi);
+            c[i] = (i & 1) ? hi : lo;
+        }
+    }
+    float o[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) o[i] = use_c ? fmaf(j.alpha, acc[i], j.beta * c[i]) : j.alpha * acc[i];
+    char* dptr = static_cast<char*>(j.D) + (base_d + m) * Out<TD>::kBytes;
+    if (m + 32 <= j.M && (reinterpret_cast<uintptr_t>(dptr) & 15) == 0) {
+        if constexpr (sizeof(TD) == 4) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                reinterpret_cast<float4*>(dptr)[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+        } else {
+            constexpr int is_half = std::is_same<TD, __half>::value ? 1 : 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                reinterpret_cast<uint4*>(dptr)[q] =
+                    make_uint4(pack2(o[8 * q], o[8 * q + 1], is_half, trunc), pack2(o[8 * q + 2], o[8 * q + 3], is_half, trunc),
+                               pack2(o[8 * q + 4], o[8 * q + 5], is_half, trunc),
+                               pack2(o[8 * q + 6], o[8 * q + 7], is_half, trunc));
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 32; ++i)
+            if (m + i < j.M) Out<TD>::store(j.D, base_d + m + i, o[i], trunc);
+    }
+}
+
 // Hand a drained TMEM buffer back to the MMA issuer: one arrival per epilogue warp, on the leader
 // CTA's barrier (a remote arrival when this CTA is the peer of a pair).
 template <int CG>
@@ -783,17 +861,24 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             const uint32_t tbase = tmem_base + lane_off + mbuf * static_cast<uint32_t>(p.bm);
             if (ok) ptx::tc_fence_after();
             if (j.nsplit == 1) {
+                // C of chunk c+1 is loaded while chunk c is drained and stored
+                uint32_t cnext[32];
+                if (ok && row_ok) load_c_chunk<TD>(j, base_c, j.m0, cnext);
                 for (int c = 0; c < chunks && ok; ++c) {
+                    uint32_t ccur[32];
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) ccur[i] = cnext[i];
+                    const int m = j.m0 + c * 32;
+                    if (row_ok && c + 1 < chunks) load_c_chunk<TD>(j, base_c, m + 32, cnext);
                     uint32_t r[32];
                     __syncwarp();
                     ptx::tmem_ld32(tbase + c * 32, r);
                     if (c == chunks - 1) release_tmem<CG>(&tempty[mbuf], lane);
-                    const int m = j.m0 + c * 32;
                     if (row_ok && m < j.M) {
                         float v[32];
 #pragma unroll
                         for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-                        store_chunk<TD>(j, base_c, base_d, m, v, p.out_trunc);
+                        store_chunk_pre<TD>(j, base_d, m, v, ccur, p.out_trunc);
                     }
                 }
             } else {

@@ -219,11 +219,14 @@ void tc_heuristic(const tl_handle* h, const tl_gemm_problem& p, int kernel, tl_g
     s->macro_tile0 = bm;
     s->macro_tile1 = kTcTileN * cg;
     s->depth_u = W;
-    s->stages = max_stages(bm / cg, h->smem_optin);
+    // measured on GB300: beyond ~6 stages (about 190 KB in flight) a deeper ring gains nothing
+    s->stages = std::min(6, max_stages(bm / cg, h->smem_optin));
     s->wave_tile0 = 0;
     s->wave_tile1 = 0;
     s->split_k = split;
-    s->raster = tiles_n > 8 ? 8 : 0;
+    // operands of up to ~64 MB stay L2-resident, where linear tile order measured best
+    const int64_t op_bytes = (p.m * p.k + p.n * p.k) * dtype_bytes(in);
+    s->raster = (tiles_n > 8 && op_bytes > (int64_t(96) << 20)) ? 8 : 0;
     s->ctas = 0;
 }
 
