@@ -52,10 +52,16 @@ WORKLOADS = {
     "bf16_480x1024x4096": dict(dtype="bf16", m=480, n=1024, k=4096, lay="NN", alpha=1.0, beta=0.5, seed=1,
                                dist="normal"),
     "bf16x3_8192": dict(dtype="fp32", m=8192, n=8192, k=8192, lay="NN", alpha=1.0, beta=0.0, seed=2,
-                        dist="uniform", kernel="bf16x3"),
+                        dist="uniform", kernel="bf16x3", steps=300),
+    "bf16x6_8192": dict(dtype="fp32", m=8192, n=8192, k=8192, lay="NN", alpha=1.0, beta=0.0, seed=2,
+                        dist="uniform", kernel="bf16x6", steps=200),
     "simt_fp32_8192": dict(dtype="fp32", m=8192, n=8192, k=8192, lay="NN", alpha=1.0, beta=0.0, seed=2,
-                           dist="uniform", kernel="simt"),
-    "fp8_8192": dict(dtype="fp8", m=8192, n=8192, k=8192, lay="TN", alpha=1.0, beta=0.0, seed=2, dist="normal"),
+                           dist="uniform", kernel="simt", steps=50),
+    "grouped256": dict(kind="grouped", dtype="bf16", count=256, seed=3, lay="NN", alpha=1.0, beta=0.0,
+                       steps=1000),
+    "fwdbwd": dict(kind="fwdbwd", dtype="bf16", m=4096, k=1024, n=4096, seed=4),
+    "fp8_8192": dict(dtype="fp8", m=8192, n=8192, k=8192, lay="TN", alpha=1.0, beta=0.0, seed=2, dist="normal",
+                     steps=2000),
     "simt_fp32_480x512x512": dict(dtype="fp32", m=480, n=512, k=512, lay="NN", alpha=1.0, beta=0.0, seed=0,
                                   dist="uniform", kernel="simt"),
 }
@@ -341,6 +347,11 @@ def run_gpu(args, w, name):
     torch.cuda.synchronize()
     mark0 = clocks.mark()
     launches0 = h.launch_count()
+    # a split-kernel step is pre-pass + GEMM: time the GEMM kernel itself with an event pair per launch
+    multi = kernel in ("bf16x3", "bf16x6")
+    if multi:
+        h.set_kernel_timing(True)
+        h.kernel_timing(reset=True)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t_wall = time.perf_counter()
     ev0.record(stream)
@@ -360,7 +371,11 @@ def run_gpu(args, w, name):
     total_flops = sum_over_ranks(flops * args.steps, world)
     value = total_flops / (ms_max / 1e3) / 1e12
     ms_per_step = ms_max / args.steps
-    kernel_ms = ms_total / args.steps / max(1, launches // max(1, args.steps))
+    kernel_ms = ms_total / args.steps
+    if multi:
+        kms, kn = h.kernel_timing(reset=True)
+        h.set_kernel_timing(False)
+        kernel_ms = kms / max(1, kn)
 
     # accuracy of the benchmarked result against an FP64 host oracle (numpy float64 matmul)
     err = None
@@ -378,7 +393,9 @@ def run_gpu(args, w, name):
     clocks.stop()
     clk = clocks.summary(mark0, mark1)
     peaks = load_peaks()
-    achieved = flops / (kernel_ms / 1e3) / 1e12
+    nterms = {"bf16x3": 3, "bf16x6": 6}.get(kernel, 1)
+    # tensor work actually executed: the split paths run nterms bf16 products per output
+    achieved = nterms * flops / (kernel_ms / 1e3) / 1e12
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 6), "higher_is_better": True,
@@ -390,15 +407,21 @@ def run_gpu(args, w, name):
                    if nsets > 1 else "inputs larger than L2",
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
         "roofline": {"bound": "tensor" if kernel != "simt" else "fp32-pipe", "achieved": round(achieved, 2),
-                     "peak": peaks["bf16_tflops"] * (2 if dtype == "fp8" else 1) if kernel != "simt" else None,
+                     "peak": (peaks["bf16_tflops"] * (2 if dtype == "fp8" else 1)) if kernel != "simt"
+                     else round(nominal_fp32_tflops(), 1),
                      "unit": "TFLOP/s", "frac": None, "traffic": None,
-                     "peak_source": peaks["source"] + (" bf16 burst" + (" x2 (fp8 dense = 2x bf16)" if dtype == "fp8"
-                                                                         else "")),
+                     "peak_source": (peaks["source"] + " bf16 burst" + (" x2 (fp8 dense = 2x bf16)" if dtype == "fp8"
+                                                                          else "")) if kernel != "simt"
+                     else "nominal FP32 FMA rate: SMs x 128 lanes x 2 x max SM clock",
                      "kernel_ms": round(kernel_ms, 6)},
         "clocks": clk, "gpu_launches": launches, "wall_s_timed": round(t_wall, 4),
     }
     if line["roofline"]["peak"]:
         line["roofline"]["frac"] = round(achieved / line["roofline"]["peak"], 4)
+    if nterms > 1:
+        line["roofline"]["note"] = (f"{kernel}: {nterms} bf16 tensor products per output; achieved counts them all "
+                                    f"over the GEMM kernel's own event-timed duration; value counts 2*m*n*k once "
+                                    f"over the whole step (fp32 split pre-pass + GEMM)")
     tag = {"bf16": "bf16", "fp16": "fp16", "fp8": "fp8", "fp32": kernel}[dtype]
     traffic = profile_traffic(f"tc_gemm_{tag}_{m}") if kernel != "simt" else profile_traffic(f"simt_{m}")
     if traffic:
@@ -412,6 +435,18 @@ def run_gpu(args, w, name):
         line["cpu_baseline"] = cpu_baseline(w, A, B, dtype, target_s=args.cpu_seconds)
     h.close()
     return line if rank == 0 else None
+
+
+def nominal_fp32_tflops():
+    import torch
+    prop = torch.cuda.get_device_properties(torch.cuda.current_device())
+    max_mhz = 2070.0
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            max_mhz = float(json.load(f).get("sm_max_mhz", max_mhz))
+    except Exception:
+        pass
+    return prop.multi_processor_count * 128 * 2 * max_mhz * 1e6 / 1e12
 
 
 def alg_bytes(w):
@@ -493,6 +528,266 @@ def run_e2e(h, p, sol, base, dC, m, n, tdt, stream, steps, world):
             "path": "pinned host -> tl_memcpy_h2d -> tl_gemm -> tl_memcpy_d2h, one stream"}
 
 
+def grouped_sizes(seed, count):
+    """M = 16*U{4..128} for all problems, then N likewise, then K = 64*U{1..64} (numpy PCG64)."""
+    g = np.random.default_rng(seed)
+    M = 16 * g.integers(4, 129, count)
+    N = 16 * g.integers(4, 129, count)
+    K = 64 * g.integers(1, 65, count)
+    return [(int(m), int(n), int(k)) for m, n, k in zip(M, N, K)]
+
+
+def run_grouped(args, w, name):
+    """256 independent bf16 GEMMs in one persistent launch (tile picked by tl_tune_grouped), replayed from a
+    CUDA graph; one step = one replay.  Entries N(0,1) from torch's generator seeded 3 on the device."""
+    import torch
+    import tensilelite_gb300 as tl
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    h = tl.Handle()
+    sizes = grouped_sizes(w["seed"], w["count"])
+    gen = torch.Generator(device="cuda").manual_seed(w["seed"])
+    probs, A, B, D = [], [], [], []
+    for (m, n, k) in sizes:
+        A.append(torch.randn(m * k, device="cuda", generator=gen).to(torch.bfloat16))
+        B.append(torch.randn(k * n, device="cuda", generator=gen).to(torch.bfloat16))
+        D.append(torch.empty(m * n, device="cuda", dtype=torch.bfloat16))
+        probs.append(tl.Problem.make(m, n, k, dtype="bf16", alpha=w["alpha"], beta=w["beta"], kernel="tcgen05"))
+    flops = sum(2.0 * m * n * k for m, n, k in sizes)
+    sol, tuned_ms = h.tune_grouped(probs, D, None, A, B, reps=3)
+    plan = h.grouped_plan(probs, D, None, A, B, solution=sol)
+    stream = torch.cuda.Stream()
+    graph = plan.capture(stream)
+    clocks = ClockSampler(local)
+    clocks.start()
+    for _ in range(args.warmup):
+        graph.launch(stream)
+    stream.synchronize()
+    h.device_status(stream)
+    barrier(world)
+    mark0 = clocks.mark()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = h.launch_count()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        graph.launch(stream)
+    ev1.record(stream)
+    ev1.synchronize()
+    mark1 = clocks.mark()
+    h.device_status(stream)
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
+    value = sum_over_ranks(flops * args.steps, world) / (ms / 1e3) / 1e12
+    # e2e: host operands in, results out, through the public API (plan launch), every step
+    e2e = None
+    if args.e2e_steps > 0:
+        hA = [a.cpu().pin_memory() for a in A]
+        hB = [b.cpu().pin_memory() for b in B]
+        hD = [torch.empty(d.numel(), dtype=torch.bfloat16).pin_memory() for d in D]
+        L = tl.lib()
+        sp = stream.cuda_stream
+        bi = sum(x.numel() * 2 for x in hA + hB)
+        bo = sum(x.numel() * 2 for x in hD)
+
+        def step():
+            for ha, da in zip(hA, A):
+                tl.check(L.tl_memcpy_h2d(da.data_ptr(), ha.data_ptr(), ha.numel() * 2, sp))
+            for hb, db in zip(hB, B):
+                tl.check(L.tl_memcpy_h2d(db.data_ptr(), hb.data_ptr(), hb.numel() * 2, sp))
+            plan.launch(stream)
+            for hd, dd in zip(hD, D):
+                tl.check(L.tl_memcpy_d2h(hd.data_ptr(), dd.data_ptr(), hd.numel() * 2, sp))
+        step()
+        stream.synchronize()
+        # every step moves ~2 GB over the host link: a few steps are enough
+        esteps = max(1, min(args.e2e_steps, 10))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(esteps):
+            step()
+        e1.record(stream)
+        e1.synchronize()
+        ems = max_over_ranks(e0.elapsed_time(e1), world)
+        e2e = {"value": round(sum_over_ranks(flops * esteps, world) / (ems / 1e3) / 1e12, 3),
+               "unit": "TFLOP/s", "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo),
+               "steps": esteps, "path": "pinned host -> tl_memcpy_h2d x512 -> tl_grouped_plan_launch -> "
+                                                 "tl_memcpy_d2h x256, one stream"}
+    clocks.stop()
+    peaks = load_peaks()
+    fl, tiles, psol = plan.info()
+    kernel_ms = ms / args.steps
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(kernel_ms, 6), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16",
+            "data": f"synthetic: sizes numpy PCG64 seed {w['seed']}; entries N(0,1) torch CUDA generator seed {w['seed']}",
+            "config": {"workload": f"{name}: {w['count']} bf16 NN GEMMs, M,N in 16*[4,128], K in 64*[1,64], "
+                                   f"one persistent launch replayed from a CUDA graph",
+                       "problems": w["count"], "total_flop": flops, "tiles": tiles, "solution": psol.as_dict(),
+                       "tuned_ms": round(tuned_ms, 4), "l2": f"operands {sum(a.numel() + b.numel() for a, b in zip(A, B)) * 2 / 2**30:.1f} GiB > L2",
+                       "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "roofline": {"bound": "tensor", "achieved": round(value / max(world, 1), 2), "peak": peaks["bf16_tflops"],
+                         "unit": "TFLOP/s", "frac": round(value / max(world, 1) / peaks["bf16_tflops"], 4),
+                         "traffic": None, "peak_source": peaks["source"] + " bf16 burst", "kernel_ms": round(kernel_ms, 6)},
+            "clocks": clocks.summary(mark0, mark1), "gpu_launches": h.launch_count() - l0 or args.steps}
+    if e2e:
+        line["e2e"] = e2e
+    if rank == 0 and not args.no_cpu:
+        m, n, k = sizes[0]
+        wl = dict(dtype="bf16", m=m, n=n, k=k, lay="NN", alpha=1.0, beta=0.0, seed=w["seed"], dist="normal")
+        Ah = A[0].float().cpu().numpy()
+        Bh = B[0].float().cpu().numpy()
+        cb = cpu_baseline(wl, Ah, Bh, "fp32", target_s=args.cpu_seconds)
+        cb["sample"] = "problem 0 of the group: " + cb["sample"]
+        line["cpu_baseline"] = cb
+    plan.close()
+    graph.close()
+    h.close()
+    return line if rank == 0 else None
+
+
+def run_fwdbwd(args, w, name):
+    """Y = X W forward and dX = dY W^T, dW = X^T dY backward through tensilelite_gb300.matmul (autograd);
+    one step = forward + backward (3 GEMM launches).  value: the step captured once in a CUDA graph
+    (torch.cuda.graph around the autograd calls) and replayed; eager: the same step called from Python."""
+    import torch
+    import tensilelite_gb300 as tl
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    M, K, N = w["m"], w["k"], w["n"]
+    g = np.random.default_rng(w["seed"])
+    Xh = (g.standard_normal(M * K) * 0.02).astype(np.float32).reshape(M, K)
+    Wh = (g.standard_normal(K * N) * 0.02).astype(np.float32).reshape(K, N)
+    dYh = g.standard_normal(M * N).astype(np.float32).reshape(M, N)
+    X = torch.from_numpy(Xh).cuda().to(torch.bfloat16).requires_grad_()
+    W = torch.from_numpy(Wh).cuda().to(torch.bfloat16).requires_grad_()
+    dY = torch.from_numpy(dYh).cuda().to(torch.bfloat16)
+    h = tl.default_handle()
+    flops = 3 * 2.0 * M * N * K
+
+    def step():
+        X.grad = None
+        W.grad = None
+        Y = tl.matmul(X, W)
+        Y.backward(dY)
+        return Y
+
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    h.device_status()
+
+    # eager: Python + autograd per step; kernel time from an event pair around each GEMM launch
+    eager_steps = min(args.steps, 2000)
+    h.set_kernel_timing(True)
+    h.kernel_timing(reset=True)
+    l0 = h.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(eager_steps):
+        step()
+    ev1.record()
+    ev1.synchronize()
+    eager_ms = ev0.elapsed_time(ev1) / eager_steps
+    eager_launches = (h.launch_count() - l0) / eager_steps
+    kms, kn = h.kernel_timing(reset=True)
+    h.set_kernel_timing(False)
+    kernel_ms_per_step = kms / max(1, kn) * eager_launches
+
+    # graph: the same three launches captured once
+    X.grad = None
+    W.grad = None
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        Yg = tl.matmul(X, W)
+        Yg.backward(dY)
+    graph.replay()
+    torch.cuda.synchronize()
+    h.device_status()
+    clocks = ClockSampler(local)
+    clocks.start()
+    for _ in range(args.warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+    barrier(world)
+    mark0 = clocks.mark()
+    ev0.record()
+    for _ in range(args.steps):
+        graph.replay()
+    ev1.record()
+    ev1.synchronize()
+    mark1 = clocks.mark()
+    h.device_status()
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
+    value = sum_over_ranks(flops * args.steps, world) / (ms / 1e3) / 1e12
+    # FP64 reference gradients at full size
+    Xd, Wd, dYd = X.detach().double(), W.detach().double(), dY.double()
+    err = {}
+    for nm, got, ref in (("Y", Yg, Xd @ Wd), ("dX", X.grad, dYd @ Wd.T), ("dW", W.grad, Xd.T @ dYd)):
+        err[nm] = float((got.detach().double() - ref).abs().max() / ref.abs().max())
+    e2e = None
+    if args.e2e_steps > 0:
+        hX = torch.from_numpy(Xh).to(torch.bfloat16).pin_memory()
+        hW = torch.from_numpy(Wh).to(torch.bfloat16).pin_memory()
+        hdY = torch.from_numpy(dYh).to(torch.bfloat16).pin_memory()
+        hdX = torch.empty(M, K, dtype=torch.bfloat16).pin_memory()
+        hdW = torch.empty(K, N, dtype=torch.bfloat16).pin_memory()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.e2e_steps):
+            with torch.no_grad():
+                X.copy_(hX, non_blocking=True)
+                W.copy_(hW, non_blocking=True)
+                dY.copy_(hdY, non_blocking=True)
+            step()
+            hdX.copy_(X.grad, non_blocking=True)
+            hdW.copy_(W.grad, non_blocking=True)
+        e1.record()
+        e1.synchronize()
+        ems = max_over_ranks(e0.elapsed_time(e1), world)
+        e2e = {"value": round(sum_over_ranks(flops * args.e2e_steps, world) / (ems / 1e3) / 1e12, 3),
+               "unit": "TFLOP/s", "h2d_bytes_per_step": 2 * (M * K + K * N + M * N),
+               "d2h_bytes_per_step": 2 * (M * K + K * N), "steps": args.e2e_steps,
+               "path": "pinned host -> copy -> tensilelite_gb300.matmul fwd+bwd (eager) -> grads to pinned host"}
+    clocks.stop()
+    peaks = load_peaks()
+    achieved = flops / (kernel_ms_per_step / 1e3) / 1e12
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 6), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+            "data": f"synthetic: numpy PCG64 seed {w['seed']}: X, W ~ N(0,1)*0.02, dY ~ N(0,1)",
+            "config": {"workload": f"{name}: Y = X W, X {M}x{K}, W {K}x{N}, forward NN + backward TN (dX) and NT (dW)",
+                       "step": "CUDA graph replay of the captured forward+backward (3 GEMM launches)",
+                       "eager": {"value": round(flops / (eager_ms / 1e3) / 1e12, 3), "ms_per_step": round(eager_ms, 6),
+                                 "steps": eager_steps},
+                       "l2": "operands 48 MiB: L2-resident between steps (no flush)",
+                       "parallelism": "replicas" if world > 1 else "1 GPU"},
+            "roofline": {"bound": "tensor", "achieved": round(achieved, 2), "peak": peaks["bf16_tflops"],
+                         "unit": "TFLOP/s", "frac": round(achieved / peaks["bf16_tflops"], 4),
+                         "traffic": None, "peak_source": peaks["source"] + " bf16 burst",
+                         "kernel_ms_per_step": round(kernel_ms_per_step, 6),
+                         "note": "achieved over the three GEMM kernels' summed event-timed durations"},
+            "accuracy_vs_fp64": err, "clocks": clocks.summary(mark0, mark1),
+            "gpu_launches": int(round(eager_launches * args.steps))}
+    if e2e:
+        line["e2e"] = e2e
+    if rank == 0 and not args.no_cpu:
+        wl = dict(dtype="bf16", m=N, n=M, k=K, lay="NN", alpha=1.0, beta=0.0, seed=w["seed"], dist="normal")
+        # Y^T = W^T X^T column-major: A = W's storage (N x K), B = X's storage (K x M)
+        line["cpu_baseline"] = cpu_baseline(wl, W.detach().float().cpu().numpy().reshape(-1),
+                                            X.detach().float().cpu().numpy().reshape(-1), "fp32",
+                                            target_s=args.cpu_seconds)
+    return line if rank == 0 else None
+
+
 # ----------------------------------------------------------------------------------------------
 # reference arm: the reference's CPU GEMM loop (oracle port), all host threads
 # ----------------------------------------------------------------------------------------------
@@ -536,7 +831,8 @@ def run_reference(args, w, name):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: about one second of GPU work for the workload)")
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="tensilelite_gb300", choices=["tensilelite_gb300", "reference"])
     ap.add_argument("--workload", default="bf16_4096_nn", choices=sorted(WORKLOADS))
@@ -548,8 +844,21 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
+    if args.steps is None:
+        args.steps = w.get("steps", 10000)
+    kind = w.get("kind", "gemm")
     if args.impl == "reference":
+        if kind == "grouped":
+            m, n, k = grouped_sizes(w["seed"], w["count"])[0]
+            w = dict(dtype="bf16", m=m, n=n, k=k, lay="NN", alpha=1.0, beta=0.0, seed=w["seed"], dist="normal")
+        elif kind == "fwdbwd":
+            w = dict(dtype="bf16", m=w["n"], n=w["m"], k=w["k"], lay="NN", alpha=1.0, beta=0.0, seed=w["seed"],
+                     dist="normal")
         line = run_reference(args, w, args.workload)
+    elif kind == "grouped":
+        line = run_grouped(args, w, args.workload)
+    elif kind == "fwdbwd":
+        line = run_fwdbwd(args, w, args.workload)
     else:
         line = run_gpu(args, w, args.workload)
     if line is not None:

@@ -276,6 +276,17 @@ TL_API tl_status tl_timer_stop(tl_timer* timer, void* stream);
 TL_API tl_status tl_timer_elapsed_ms(tl_timer* timer, float* ms);   /* synchronises the stop */
 TL_API tl_status tl_timer_destroy(tl_timer* timer);
 
+/* Per-launch kernel timing.  The reference times every kernel launch with a start/stop event pair
+ * and blocks until the stop (StreamHip::Launch, ff_gpu_src/ff_hip_runtime.cpp:278-320, read back as
+ * kernelExeTime in SolutionCtrlBase::run_comb_kernel, ff_gpu_src/ff_gpu_test_fw.cpp:24-52).  Here,
+ * while enabled, an event pair is recorded on the launching stream around each GEMM kernel launch
+ * (tl_gemm's tensor-core or CUDA-core kernel, a grouped plan's launch; not the split/quantise
+ * pre-passes) without blocking; tl_kernel_timing waits for the recorded launches and returns the
+ * summed kernel time and the number of timed launches (reset != 0 clears both afterwards).
+ * Launches into a stream that is being captured are not timed. */
+TL_API tl_status tl_set_kernel_timing(tl_handle* handle, int enable);
+TL_API tl_status tl_kernel_timing(tl_handle* handle, double* total_ms, int64_t* launches, int reset);
+
 /* Number of library kernel launches issued through this handle since creation. */
 TL_API tl_status tl_launch_count(tl_handle* handle, int64_t* launches);
 

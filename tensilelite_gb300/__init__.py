@@ -154,6 +154,8 @@ def lib():
         "tl_timer_create": [ctypes.POINTER(_vp)], "tl_timer_start": [_vp, _vp], "tl_timer_stop": [_vp, _vp],
         "tl_timer_elapsed_ms": [_vp, ctypes.POINTER(f32)], "tl_timer_destroy": [_vp],
         "tl_launch_count": [_vp, ctypes.POINTER(i64)], "tl_device_status": [_vp, _vp],
+        "tl_set_kernel_timing": [_vp, i32],
+        "tl_kernel_timing": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(i64), i32],
         "tl_set_wait_timeout": [_vp, ctypes.c_uint32],
     }
     for name, argt in sig.items():
@@ -271,6 +273,16 @@ class Handle:
         n = ctypes.c_int64()
         check(lib().tl_launch_count(self._h, ctypes.byref(n)))
         return n.value
+
+    def set_kernel_timing(self, enable: bool):
+        """Record an event pair around every GEMM kernel launch (see tl_set_kernel_timing)."""
+        check(lib().tl_set_kernel_timing(self._h, 1 if enable else 0))
+
+    def kernel_timing(self, reset=True):
+        """(summed kernel milliseconds, timed launches) since the last reset; waits for them."""
+        ms, n = ctypes.c_double(), ctypes.c_int64()
+        check(lib().tl_kernel_timing(self._h, ctypes.byref(ms), ctypes.byref(n), 1 if reset else 0))
+        return ms.value, n.value
 
     def device_status(self, stream=None):
         check(lib().tl_device_status(self._h, _stream_ptr(stream)))
@@ -402,17 +414,27 @@ def gemm_colmajor(A, B, m, n, k, *, C=None, D=None, alpha=1.0, beta=0.0, trans_a
     return D
 
 
+_MM_PROBLEMS = {}
+
+
 def _mm_rowmajor(X, W, trans_x=False, trans_w=False):
-    """Row-major X(M,K) @ W(K,N) through the column-major kernels (op flags on the stored tensors)."""
+    """Row-major X(M,K) @ W(K,N) through the column-major kernels (op flags on the stored tensors).
+    The problem descriptor is built once per (dtype, layout, shape) and reused: the per-call host cost
+    is then the two tensor-map encodings and the launch."""
     import torch
     Xs, Ws = X.contiguous(), W.contiguous()
     M = Xs.shape[1] if trans_x else Xs.shape[0]
     K = Xs.shape[0] if trans_x else Xs.shape[1]
     N = Ws.shape[0] if trans_w else Ws.shape[1]
+    key = (X.dtype, trans_x, trans_w, M, N, K)
+    p = _MM_PROBLEMS.get(key)
+    if p is None:
+        # Y (row-major M x N) == column-major N x M:  Y^T = op(W)^T op(X)^T
+        p = Problem.make(N, M, K, dtype=torch_dtype_code(X.dtype), trans_a=trans_w, trans_b=trans_x,
+                         lda=Ws.shape[1], ldb=Xs.shape[1], ldd=N)
+        _MM_PROBLEMS[key] = p
     Y = torch.empty((M, N), dtype=X.dtype, device=X.device)
-    # Y (row-major M x N) == column-major N x M:  Y^T = op(W)^T op(X)^T
-    gemm_colmajor(Ws, Xs, N, M, K, D=Y, trans_a=trans_w, trans_b=trans_x,
-                  lda=Ws.shape[1], ldb=Xs.shape[1], ldd=N)
+    default_handle().gemm(p, Y, None, Ws, Xs)
     return Y
 
 

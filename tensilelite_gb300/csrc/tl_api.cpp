@@ -37,6 +37,16 @@ struct tl_handle {
     uint64_t timeout_ns = 4000000000ull;
     std::map<std::string, tl_gemm_solution> tuned;
     std::mutex mu;
+    // Once a stream capture has recorded this handle's workspace address, a grown workspace retires
+    // the old buffer here (freed by tl_destroy) instead of freeing it under a live graph.
+    bool captured = false;
+    std::vector<void*> retired;
+    // Per-launch kernel timing: an event pair around each GEMM kernel launch, read back lazily.
+    bool timing = false;
+    std::vector<cudaEvent_t> tev;  // 2 * kTimingPairs events, start/stop interleaved
+    size_t tev_used = 0;           // events recorded since the last fold
+    double timing_ms = 0.0;
+    int64_t timing_count = 0;
 };
 
 struct tl_grouped_plan {
@@ -272,12 +282,29 @@ std::string problem_key(const tl_handle* h, const tl_gemm_problem& p)
     return buf;
 }
 
+// Set for the calling thread while tl_gemm runs on a stream that is being captured: buffers may not
+// grow then (an allocation is not capturable, and the graph would keep the old address).
+static thread_local bool t_capturing = false;
+
+tl_status grow_refused_in_capture(const char* what)
+{
+    return fail(TL_ERR_UNSUPPORTED, std::string(what) + " would have to grow during stream capture: run the same "
+                                    "problem once on this handle outside the capture first");
+}
+
+void retire_or_free(tl_handle* h, void* ptr)
+{
+    cudaDeviceSynchronize();
+    if (h->captured) h->retired.push_back(ptr);
+    else cudaFree(ptr);
+}
+
 tl_status ensure_ws(tl_handle* h, size_t bytes)
 {
     if (bytes <= h->ws_bytes) return TL_SUCCESS;
+    if (t_capturing) return grow_refused_in_capture("the workspace");
     if (h->ws) {
-        cudaDeviceSynchronize();
-        cudaFree(h->ws);
+        retire_or_free(h, h->ws);
         h->ws = nullptr;
         h->ws_bytes = 0;
     }
@@ -291,9 +318,9 @@ tl_status ensure_ws(tl_handle* h, size_t bytes)
 tl_status ensure_counters(tl_handle* h, size_t n)
 {
     if (n <= h->counters_len) return TL_SUCCESS;
+    if (t_capturing) return grow_refused_in_capture("the split-k counter array");
     if (h->counters) {
-        cudaDeviceSynchronize();
-        cudaFree(h->counters);
+        retire_or_free(h, h->counters);
         h->counters = nullptr;
         h->counters_len = 0;
     }
@@ -455,6 +482,45 @@ tl_status prepare(tl_handle* h, const tl_gemm_problem* prob, const tl_gemm_solut
     return TL_SUCCESS;
 }
 
+constexpr size_t kTimingPairs = 1024;
+
+// Adds the elapsed times of every recorded start/stop pair to the running sum (waits for the last stop).
+tl_status timing_fold(tl_handle* h)
+{
+    if (h->tev_used == 0) return TL_SUCCESS;
+    TL_CUDA_TRY(cudaEventSynchronize(h->tev[h->tev_used - 1]));
+    for (size_t i = 0; i + 1 < h->tev_used; i += 2) {
+        float ms = 0.0f;
+        TL_CUDA_TRY(cudaEventElapsedTime(&ms, h->tev[i], h->tev[i + 1]));
+        h->timing_ms += ms;
+        h->timing_count += 1;
+    }
+    h->tev_used = 0;
+    return TL_SUCCESS;
+}
+
+bool stream_capturing(cudaStream_t s)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+}
+
+// Records the start event of a timed launch; returns false when timing is off (or the stream is being
+// captured, where an event record would become a graph node instead of a timestamp).
+bool timing_begin(tl_handle* h, cudaStream_t s)
+{
+    if (!h->timing || h->tev.empty() || stream_capturing(s)) return false;
+    if (h->tev_used + 2 > h->tev.size() && timing_fold(h) != TL_SUCCESS) return false;
+    return cudaEventRecord(h->tev[h->tev_used], s) == cudaSuccess;
+}
+
+void timing_end(tl_handle* h, cudaStream_t s, bool started, tl_status launch_status)
+{
+    if (!started) return;
+    if (launch_status == TL_SUCCESS && cudaEventRecord(h->tev[h->tev_used + 1], s) == cudaSuccess)
+        h->tev_used += 2;
+}
+
 tl_status enqueue(tl_handle* h, const Prepared& P, cudaStream_t s)
 {
     const tl_gemm_problem& p = P.p;
@@ -473,7 +539,10 @@ tl_status enqueue(tl_handle* h, const Prepared& P, cudaStream_t s)
         L.lda = p.lda; L.ldb = p.ldb; L.ldc = p.ldc; L.ldd = p.ldd;
         L.sa = p.stride_a; L.sb = p.stride_b; L.sc = p.stride_c; L.sd = p.stride_d;
         L.alpha = alpha; L.beta = p.beta;
-        return simt_gemm_launch(L, s, &h->launches);
+        const bool timed = timing_begin(h, s);
+        const tl_status st = simt_gemm_launch(L, s, &h->launches);
+        timing_end(h, s, timed, st);
+        return st;
     }
     TcLaunch L;
     memset(&L, 0, sizeof(L));
@@ -520,7 +589,10 @@ tl_status enqueue(tl_handle* h, const Prepared& P, cudaStream_t s)
     L.counters_len = h->counters_len;
     L.tail_split = P.s.tail_split;
     L.sm_count = h->sm_count;
-    return tc_gemm_launch(L, s, &h->launches);
+    const bool timed = timing_begin(h, s);
+    const tl_status st = tc_gemm_launch(L, s, &h->launches);
+    timing_end(h, s, timed, st);
+    return st;
 }
 
 // ---- tuner ------------------------------------------------------------------------------------------
@@ -728,6 +800,8 @@ TL_API tl_status tl_destroy(tl_handle* h)
     cudaDeviceSynchronize();
     if (h->ws) cudaFree(h->ws);
     if (h->counters) cudaFree(h->counters);
+    for (void* r : h->retired) cudaFree(r);
+    for (cudaEvent_t e : h->tev) cudaEventDestroy(e);
     if (h->d_err) cudaFree(h->d_err);
     delete h;
     return TL_SUCCESS;
@@ -803,7 +877,10 @@ TL_API tl_status tl_gemm(tl_handle* h, const tl_gemm_problem* p, const tl_gemm_s
 {
     if (!h) return fail(TL_ERR_INVALID_ARG, "handle is NULL");
     Prepared P;
+    t_capturing = stream_capturing(S(stream));
+    if (t_capturing) h->captured = true;
     tl_status st = prepare(h, p, s, D, C, A, B, &P);
+    t_capturing = false;
     if (st != TL_SUCCESS) return st;
     return enqueue(h, P, S(stream));
 }
@@ -1017,7 +1094,10 @@ TL_API tl_status tl_grouped_plan_launch(tl_grouped_plan* pl, void* stream)
 {
     if (!pl) return fail(TL_ERR_INVALID_ARG, "plan is NULL");
     if (pl->launch.total_tiles == 0) return TL_SUCCESS;
-    return tc_grouped_launch(pl->launch, S(stream), &pl->h->launches);
+    const bool timed = timing_begin(pl->h, S(stream));
+    const tl_status st = tc_grouped_launch(pl->launch, S(stream), &pl->h->launches);
+    timing_end(pl->h, S(stream), timed, st);
+    return st;
 }
 
 TL_API tl_status tl_grouped_plan_destroy(tl_grouped_plan* pl)
@@ -1141,6 +1221,7 @@ TL_API tl_status tl_graph_capture_gemm(tl_handle* h, const tl_gemm_problem* p, c
     Prepared P;
     tl_status st = prepare(h, p, sol, D, C, A, B, &P);   // allocations happen before capture
     if (st != TL_SUCCESS) return st;
+    h->captured = true;
     cudaStream_t s = S(stream);
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCapture");
@@ -1317,6 +1398,48 @@ TL_API tl_status tl_timer_destroy(tl_timer* t)
     cudaEventDestroy(t->start);
     cudaEventDestroy(t->stop);
     delete t;
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_set_kernel_timing(tl_handle* h, int enable)
+{
+    if (!h) return fail(TL_ERR_INVALID_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lock(h->mu);
+    if (enable && h->tev.empty()) {
+        int prev = 0;
+        TL_CUDA_TRY(cudaGetDevice(&prev));
+        TL_CUDA_TRY(cudaSetDevice(h->device));
+        h->tev.resize(2 * kTimingPairs, nullptr);
+        cudaError_t ce = cudaSuccess;
+        for (auto& e : h->tev)
+            if ((ce = cudaEventCreate(&e)) != cudaSuccess) break;
+        cudaSetDevice(prev);
+        if (ce != cudaSuccess) {
+            for (auto& x : h->tev) if (x) cudaEventDestroy(x);
+            h->tev.clear();
+            return cuda_fail(ce, "cudaEventCreate");
+        }
+    }
+    if (!enable) {
+        tl_status st = timing_fold(h);
+        if (st != TL_SUCCESS) return st;
+    }
+    h->timing = enable != 0;
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_kernel_timing(tl_handle* h, double* total_ms, int64_t* launches, int reset)
+{
+    if (!h) return fail(TL_ERR_INVALID_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lock(h->mu);
+    tl_status st = timing_fold(h);
+    if (st != TL_SUCCESS) return st;
+    if (total_ms) *total_ms = h->timing_ms;
+    if (launches) *launches = h->timing_count;
+    if (reset) {
+        h->timing_ms = 0.0;
+        h->timing_count = 0;
+    }
     return TL_SUCCESS;
 }
 

@@ -441,6 +441,103 @@ def test_gemm_graph_capture(h):
     graph.close()
 
 
+def _split_case(seed, m, n, k):
+    import torch
+    case = gg.make_case("bf16", "NN", seed, m, n, k, alpha=1.0, beta=0.0)
+    A, B = gu.to_dev(case["A_bits"], "bf16"), gu.to_dev(case["B_bits"], "bf16")
+    D = torch.empty(m * n, dtype=torch.bfloat16, device="cuda")
+    p = tl.Problem.make(m, n, k, dtype="bf16", lda=case["lda"], ldb=case["ldb"], kernel="tcgen05")
+    return case, A, B, D, p
+
+
+def test_graph_survives_workspace_growth():
+    """A captured split-k GEMM keeps its workspace after a larger problem grows the handle's buffer."""
+    import torch
+    h = tl.Handle()
+    sol = tl.Solution(kernel=tl.KERNEL_TCGEN05, macro_tile0=128, macro_tile1=128, depth_u=64, stages=4, split_k=2)
+    case, A, B, D, p = _split_case(91, 256, 256, 1024)
+    s = torch.cuda.Stream()
+    graph = h.capture_gemm(p, D, None, A, B, solution=sol, stream=s)
+    # a bigger split-k problem grows the workspace (the captured buffer is retired, not freed)
+    big, A2, B2, D2, p2 = _split_case(92, 1024, 1024, 2048)
+    sol2 = tl.Solution(kernel=tl.KERNEL_TCGEN05, macro_tile0=128, macro_tile1=128, depth_u=64, stages=4, split_k=8)
+    h.gemm(p2, D2, None, A2, B2, solution=sol2, stream=s)
+    D.fill_(float("nan"))
+    graph.launch(s)
+    s.synchronize()
+    h.device_status(s)
+    assert_close(gu.mat(gu.from_dev(D, "bf16"), 256, 256, 256), gu.mat(gu.oracle_ref(case), 256, 256, 256),
+                 absprod_of(case), 1024, 1.0, 0.0, None, "bf16")
+    assert_close(gu.mat(gu.from_dev(D2, "bf16"), 1024, 1024, 1024), gu.mat(gu.oracle_ref(big), 1024, 1024, 1024),
+                 absprod_of(big), 2048, 1.0, 0.0, None, "bf16")
+    graph.close()
+    h.close()
+
+
+def test_capture_refuses_workspace_growth():
+    """Inside a stream capture a problem whose workspace is not yet allocated fails with a clear error
+    (an allocation is not capturable); after one eager call the same problem captures."""
+    import torch
+    h = tl.Handle()
+    sol = tl.Solution(kernel=tl.KERNEL_TCGEN05, macro_tile0=128, macro_tile1=128, depth_u=64, stages=4, split_k=4)
+    case, A, B, D, p = _split_case(93, 512, 512, 2048)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with pytest.raises(tl.TLError) as ei:
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                h.gemm(p, D, None, A, B, solution=sol, stream=s)
+    assert ei.value.status == tl.ERR_UNSUPPORTED
+    assert b"stream capture" in tl.lib().tl_last_error_string()
+    torch.cuda.synchronize()
+    h.gemm(p, D, None, A, B, solution=sol, stream=s)       # sizes the workspace
+    g2 = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g2, stream=s):
+            h.gemm(p, D, None, A, B, solution=sol, stream=s)
+    D.fill_(float("nan"))
+    g2.replay()
+    torch.cuda.synchronize()
+    h.device_status()
+    assert_close(gu.mat(gu.from_dev(D, "bf16"), 512, 512, 512), gu.mat(gu.oracle_ref(case), 512, 512, 512),
+                 absprod_of(case), 2048, 1.0, 0.0, None, "bf16")
+    h.close()
+
+
+def test_kernel_timing_counts_gemm_launches():
+    """tl_kernel_timing: one event pair per GEMM kernel (not the split pre-pass); the summed kernel
+    time lies inside the stream time around the same launches."""
+    import torch
+    h = tl.Handle()
+    case, A, B, D, p = _split_case(94, 1024, 1024, 1024)
+    s = torch.cuda.Stream()
+    h.gemm(p, D, None, A, B, stream=s)
+    h.set_kernel_timing(True)
+    h.kernel_timing(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(5):
+        h.gemm(p, D, None, A, B, stream=s)
+    e1.record(s)
+    ms, n = h.kernel_timing(reset=True)
+    assert n == 5
+    assert 0 < ms <= e0.elapsed_time(e1) * 1.01 + 0.01
+    # fp32 operands on the split path: 2 split launches + 1 GEMM per call, only the GEMM is timed
+    Af = torch.randn(512 * 512, device="cuda")
+    Bf = torch.randn(512 * 512, device="cuda")
+    Df = torch.empty(512 * 512, device="cuda")
+    pf = tl.Problem.make(512, 512, 512, dtype="fp32", kernel="bf16x3")
+    l0 = h.launch_count()
+    h.gemm(pf, Df, None, Af, Bf, stream=s)
+    assert h.launch_count() - l0 == 3
+    ms, n = h.kernel_timing(reset=True)
+    assert n == 1 and ms > 0
+    h.set_kernel_timing(False)
+    h.gemm(p, D, None, A, B, stream=s)
+    assert h.kernel_timing()[1] == 0
+    h.close()
+
+
 # ---------------------------------------------------------------------------- tuner, norms, autograd
 def test_tune_and_cache(h, tmp_path):
     import torch
