@@ -28,6 +28,7 @@
 #include <cuda_fp16.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 
@@ -41,8 +42,7 @@ namespace {
 struct TcKernelParams {
     CUtensorMap tmN[3], tmM[3];   // split-precision pieces 0..2 (piece 0 = the operand itself)
     const TcGroupEntry* group;
-    const int64_t* group_prefix;
-    int group_count;
+    const int4* group_units;       // per work unit: {problem, tile row, tile column, k-blocks}
     void* D;
     const void* C;
     int64_t ldd, ldc, stride_d, stride_c;
@@ -85,7 +85,14 @@ struct TileJob {
     int64_t slot;                 // split tiles: index of the tile's workspace slabs and counter
 };
 
-__device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, TileJob& j)
+// Grouped launches: the unit-table entry of work unit w (a zero entry past the end or without a group).
+__device__ __forceinline__ int4 load_unit(const TcKernelParams& p, int64_t w)
+{
+    if (p.group == nullptr || w >= p.total_work) return make_int4(0, 0, 0, 0);
+    return __ldg(p.group_units + w);
+}
+
+__device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, const int4& u, TileJob& j)
 {
     if (p.group == nullptr) {
         int64_t tile;
@@ -136,16 +143,9 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, Tile
         j.tile = tile;
         j.slot = tile - p.tail_start;
     } else {
-        // binary search: group_prefix[g] <= w < group_prefix[g+1]
-        int lo = 0, hi = p.group_count - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (p.group_prefix[mid] <= w) lo = mid; else hi = mid - 1;
-        }
-        const TcGroupEntry& e = p.group[lo];
-        const int64_t t = w - p.group_prefix[lo];
-        const int in = static_cast<int>(t / e.tiles_m);
-        const int jm = static_cast<int>(t % e.tiles_m);
+        // grouped: the unit's problem and tile come from the plan's unit table (loaded ahead by
+        // the caller); only the epilogue reads the problem's entry
+        const TcGroupEntry& e = p.group[u.x];
         j.tmN = &e.tmN;
         j.tmM = &e.tmM;
         j.D = e.D;
@@ -157,10 +157,10 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, Tile
         j.alpha = e.alpha;
         j.beta = e.beta;
         j.b = 0;
-        j.n0 = in * p.tile_rows;
-        j.m0 = jm * p.bm;
+        j.n0 = u.y * p.tile_rows;
+        j.m0 = u.z * p.bm;
         j.kb0 = 0;
-        j.kb1 = (e.K + p.kb_elems - 1) / p.kb_elems;
+        j.kb1 = u.w;
         j.split = 0;
         j.nsplit = 1;
         j.tile = w;
@@ -557,6 +557,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
     if constexpr (CG == 2) ptx::cluster_sync();     // peer barriers initialised before any remote arrive
     ptx::tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
+    // Launched as a programmatic dependent: everything above (barrier set-up, TMEM allocation,
+    // descriptor prefetch) may have run while the previous kernel in the stream was finishing.
+    // Wait for that grid to complete (its writes visible) before touching global memory, then let
+    // the next dependent grid start its own set-up as soon as SMs free up.
+    ptx::grid_dep_wait();
+    ptx::grid_dep_launch_dependents();
     const int nvirt = p.nterms;
     const uint64_t tlim = p.timeout_ns;
 
@@ -570,9 +576,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             const int n_mn = p.n_mn_major, m_mn = p.m_mn_major;
             const int nstages = p.stages;
             bool ok = true;
+            int4 u_next = load_unit(p, unit0);
             for (int64_t w = unit0; w < p.total_work && ok; w += units) {
+                const int4 u = u_next;
+                u_next = load_unit(p, w + units);      // in flight during this tile
                 TileJob j;
-                get_job(p, w, j);
+                get_job(p, w, u, j);
                 const int n0 = j.n0 + static_cast<int>(rank) * kTcTileN;
                 const int m0 = j.m0 + static_cast<int>(rank * bmc);
                 const int total = (j.kb1 - j.kb0) * nvirt;
@@ -653,9 +662,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             const uint32_t bmu = static_cast<uint32_t>(p.bm);
             const int nstages = p.stages;
             bool ok = true;
+            int4 u_next = load_unit(p, unit0);
             for (int64_t w = unit0; w < p.total_work && ok; w += units) {
+                const int4 u = u_next;
+                u_next = load_unit(p, w + units);      // in flight during this tile
                 TileJob j;
-                get_job(p, w, j);
+                get_job(p, w, u, j);
                 const int nkb = j.kb1 - j.kb0;
                 const int chunk = promo ? p.promote_kb : (nkb > 0 ? nkb : 1);
                 if (sep_small) {
@@ -756,8 +768,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
         const int chunks = p.bm / 32;
         bool ok = true;
         for (int64_t w = unit0; w < p.total_work; w += units) {
+            const int4 u = load_unit(p, w);      // the epilogue trails the MMAs: no need to load ahead
             TileJob j;
-            get_job(p, w, j);
+            get_job(p, w, u, j);
             j.n0 += static_cast<int>(rank) * kTcTileN;
             j.slot = j.slot * CG + rank;              // split-k slabs and counters per CTA half
             const int n = j.n0 + row;
@@ -931,6 +944,16 @@ EncodeTiledFn get_encode_fn()
     return fn;
 }
 
+// Programmatic dependent launch for the tensor-core kernel: on unless TL_PDL=0 in the environment.
+bool pdl_enabled()
+{
+    static const bool on = [] {
+        const char* e = getenv("TL_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 template <int KIND, typename TD, int CG>
 tl_status launch_kernel(const TcKernelParams& kp, int grid, size_t smem, cudaStream_t stream)
 {
@@ -941,26 +964,34 @@ tl_status launch_kernel(const TcKernelParams& kp, int grid, size_t smem, cudaStr
         attr_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     });
     if (attr_err != cudaSuccess) return cuda_fail(attr_err, "cudaFuncSetAttribute(tc_gemm_kernel)");
-    if constexpr (CG == 1) {
-        kern<<<grid, kTcThreads, smem, stream>>>(kp);
-    } else {
-        cudaLaunchConfig_t cfg;
-        memset(&cfg, 0, sizeof(cfg));
-        cfg.gridDim = dim3(static_cast<unsigned>(grid), 1, 1);
-        cfg.blockDim = dim3(kTcThreads, 1, 1);
-        cfg.dynamicSmemBytes = smem;
-        cfg.stream = stream;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = 2;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        cudaError_t e = cudaLaunchKernelEx(&cfg, kern, kp);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchKernelEx(tc_gemm_kernel, cluster of 2)");
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3(static_cast<unsigned>(grid), 1, 1);
+    cfg.blockDim = dim3(kTcThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[2];
+    int na = 0;
+    if (pdl_enabled()) {
+        // programmatic dependent launch: this grid's prologue may overlap the previous kernel's tail
+        // (the kernel waits for the previous grid before its first global-memory access)
+        attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[na].val.programmaticStreamSerializationAllowed = 1;
+        ++na;
     }
-    cudaError_t e = cudaGetLastError();
+    if constexpr (CG == 2) {
+        attr[na].id = cudaLaunchAttributeClusterDimension;
+        attr[na].val.clusterDim.x = 2;
+        attr[na].val.clusterDim.y = 1;
+        attr[na].val.clusterDim.z = 1;
+        ++na;
+    }
+    cfg.attrs = attr;
+    cfg.numAttrs = na;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, kp);
+    if (e != cudaSuccess) return cuda_fail(e, CG == 2 ? "cudaLaunchKernelEx(tc_gemm_kernel, cluster of 2)"
+                                                      : "cudaLaunchKernelEx(tc_gemm_kernel)");
+    e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "tc_gemm_kernel launch");
     return TL_SUCCESS;
 }
@@ -1215,8 +1246,7 @@ tl_status tc_grouped_launch(const TcGroupLaunch& G, cudaStream_t stream, int64_t
     TcKernelParams kp;
     memset(&kp, 0, sizeof(kp));
     kp.group = G.d_entries;
-    kp.group_prefix = G.d_tile_prefix;
-    kp.group_count = G.count;
+    kp.group_units = G.d_units;
     kp.bm = G.bm;
     kp.stages = G.stages;
     kp.split_k = 1;

@@ -31,6 +31,19 @@ __device__ __forceinline__ void fence_mbar_init()
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+// Programmatic dependent launch: block until the prerequisite grid has completed and its memory
+// operations are visible (returns at once when the launch has no programmatic dependency).
+__device__ __forceinline__ void grid_dep_wait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+// Allow the dependent grid to be scheduled once every CTA of this grid has issued this (or exited).
+__device__ __forceinline__ void grid_dep_launch_dependents()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ void fence_proxy_async_smem()
 {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

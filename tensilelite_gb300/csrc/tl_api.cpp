@@ -52,7 +52,7 @@ struct tl_handle {
 struct tl_grouped_plan {
     tl_handle* h = nullptr;
     tl::TcGroupEntry* d_entries = nullptr;
-    int64_t* d_prefix = nullptr;
+    int4* d_units = nullptr;       // per work unit {problem, tile row, tile column, k-blocks}
     tl::TcGroupLaunch launch{};
     tl_gemm_solution sol{};
     double flops = 0.0;
@@ -184,59 +184,109 @@ void simt_solution(tl_gemm_solution* s)
 bool m_mn_major(const tl_gemm_problem& p) { return p.trans_a == TL_OP_N; }   // A[m + k*lda]
 bool n_mn_major(const tl_gemm_problem& p) { return p.trans_b == TL_OP_T; }   // B[n + k*ldb]
 
+tl_status check_tc_solution(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solution& s);
+
+// Modelled duration of one tensor-core launch, in SM clocks.  Per 128-byte k-block a CTA needs the
+// larger of its MMA time (656 clocks for a 128 x 256 x 64 bf16 block, proportional to the tile
+// width, floor 300) and its operand bytes over the L2-to-SM bandwidth (about 38 bytes per clock per
+// SM with every SM loading, more when fewer do) -- measured on GB300, the second term decides most
+// shapes, which is why a CTA pair (half the m-side operand per SM) wins even on a partial wave.
+// Tiles run in persistent waves; a last wave that would leave half the workers idle is split along
+// k as the launch does; a tile's epilogue overlaps the next tile's main loop unless it is longer.
+double tc_cost(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solution& s, int in_dtype)
+{
+    const int W = row_elems(in_dtype);
+    const int cg = s.macro_tile1 / kTcTileN;
+    const int bm = s.macro_tile0;
+    const int64_t num_kb = std::max<int64_t>(1, (p.k + W - 1) / W);
+    const int64_t tiles = ((p.n + kTcTileN * cg - 1) / (kTcTileN * cg)) * ((p.m + bm - 1) / bm) * p.batch;
+    const int64_t workers = std::max<int64_t>(1, h->sm_count / cg);
+    const int64_t split = std::max<int64_t>(1, s.split_k);
+    const int64_t units = tiles * split;
+    const double mma_kb = std::max(656.0 * bm / 256.0, 300.0);
+    const double bytes_kb = static_cast<double>(kTcTileN) * kTcRowBytes + static_cast<double>(bm) / cg * kTcRowBytes;
+    auto per_kb = [&](double active_ctas) {
+        const double bw = std::min(64.0, 38.0 * h->sm_count / std::max(1.0, active_ctas));
+        return std::max(mma_kb, bytes_kb / bw);
+    };
+    const int out_b = dtype_bytes(p.dtype_d);
+    const double epi = static_cast<double>(kTcTileN) * bm / cg * (out_b + (p.beta != 0.0f ? out_b : 0)) / 27.0;
+    auto unit_time = [&](double kb, double active_ctas) { return std::max(kb * per_kb(active_ctas), epi) + 1500.0; };
+    const double kb_unit = static_cast<double>(num_kb) / split;
+    const int64_t full = units / workers, rem = units % workers;
+    double cost = 6000.0 + epi;      // launch, prologue, the last tile's epilogue
+    cost += static_cast<double>(full) * unit_time(kb_unit, static_cast<double>(std::min(units, workers)) * cg);
+    if (rem > 0) {
+        if (split == 1 && s.tail_split != 1 && tiles > workers && 2 * rem <= workers) {
+            int64_t S = std::min<int64_t>(std::min<int64_t>(workers / rem, num_kb), 8);
+            if (s.tail_split > 1) S = std::min<int64_t>(s.tail_split, num_kb);
+            cost += unit_time(static_cast<double>(num_kb) / S, static_cast<double>(rem * S * cg)) + 2000.0 + epi;
+        } else {
+            cost += unit_time(kb_unit, static_cast<double>(rem * cg));
+        }
+    }
+    if (split > 1) cost += 3000.0 + epi;     // partials round trip and the last arriver's reduction
+    return cost;
+}
+
 void tc_heuristic(const tl_handle* h, const tl_gemm_problem& p, int kernel, tl_gemm_solution* s)
 {
     memset(s, 0, sizeof(*s));
     s->kernel = kernel;
     const int in = is_split(kernel) ? TL_DTYPE_BF16 : p.dtype_a;
     const int W = row_elems(in);
-    const bool mmn = m_mn_major(p);
     const int64_t tiles_n = (p.n + kTcTileN - 1) / kTcTileN;
     const int64_t num_kb = (p.k + W - 1) / W;
-    int bm = 256;
-    const int cands[3] = {256, 128, 64};
-    for (int c : cands) {
-        if (mmn && c % W) continue;
-        bm = c;
-        const int64_t tiles = tiles_n * ((p.m + c - 1) / c) * p.batch;
-        if (tiles >= h->sm_count) break;
-        if (c == 64 || (mmn && c == W)) break;
-    }
-    if (mmn && bm % W) bm = 2 * W > 256 ? W : 2 * W;
-    const int64_t tiles = tiles_n * ((p.m + bm - 1) / bm) * p.batch;
-    int split = 1;
-    if (tiles < h->sm_count / 2 && num_kb >= 8) {
-        split = static_cast<int>(std::min<int64_t>(h->sm_count / std::max<int64_t>(1, tiles), num_kb / 4));
-        split = std::max(1, std::min(split, 16));
-    }
-    if (is_split(kernel)) {
-        // FP32-accurate paths: 128-wide tiles so the dominant product can be promoted out of TMEM
-        // every 256 k (the chain length sets the tensor-core accumulation error)
-        bm = 128;
-        s->promote_k = 256;
-        const int64_t t128 = tiles_n * ((p.m + 127) / 128) * p.batch;
-        split = 1;
-        if (t128 < h->sm_count / 2 && num_kb >= 8)
-            split = std::max(1, static_cast<int>(std::min<int64_t>(std::min<int64_t>(h->sm_count / std::max<int64_t>(1, t128),
-                                                                                     num_kb / 4), 16)));
-    }
-    int cg = 1;
-    if (!is_split(kernel) && bm == 256 && split == 1) {
-        // large problems: a CTA pair per 256 x 256 tile halves the n-side operand each SM stages
-        const int64_t pair_tiles = ((p.n + 2 * kTcTileN - 1) / (2 * kTcTileN)) * ((p.m + 255) / 256) * p.batch;
-        if (pair_tiles >= h->sm_count / 2 && (!mmn || (bm / 2) % W == 0)) cg = 2;
-    }
-    s->macro_tile0 = bm;
-    s->macro_tile1 = kTcTileN * cg;
     s->depth_u = W;
-    // measured on GB300: beyond ~6 stages (about 190 KB in flight) a deeper ring gains nothing
-    s->stages = std::min(6, max_stages(bm / cg, h->smem_optin));
-    s->wave_tile0 = 0;
-    s->wave_tile1 = 0;
-    s->split_k = split;
     // operands of up to ~64 MB stay L2-resident, where linear tile order measured best
     const int64_t op_bytes = (p.m * p.k + p.n * p.k) * dtype_bytes(in);
     s->raster = (tiles_n > 8 && op_bytes > (int64_t(96) << 20)) ? 8 : 0;
+    if (is_split(kernel)) {
+        // FP32-accurate paths: 128-wide tiles so the dominant product can be promoted out of TMEM
+        // every 256 k (the chain length sets the tensor-core accumulation error)
+        s->macro_tile0 = 128;
+        s->macro_tile1 = kTcTileN;
+        s->promote_k = 256;
+        const int64_t t128 = tiles_n * ((p.m + 127) / 128) * p.batch;
+        int split = 1;
+        if (t128 < h->sm_count / 2 && num_kb >= 8)
+            split = std::max(1, static_cast<int>(std::min<int64_t>(std::min<int64_t>(h->sm_count / std::max<int64_t>(1, t128),
+                                                                                     num_kb / 4), 16)));
+        s->split_k = split;
+        s->stages = std::min(6, max_stages(128, h->smem_optin));
+        return;
+    }
+    // the legal tile with the least modelled time
+    double best = 0.0;
+    bool have = false;
+    tl_gemm_solution c = *s;
+    for (int cg : {2, 1})
+        for (int bm : {256, 128, 192, 64})
+            for (int split : {1, 2, 3, 4, 6, 8, 12, 16}) {
+                if (split > 1 && (split > num_kb / 2 || split > 16)) continue;
+                c.macro_tile0 = bm;
+                c.macro_tile1 = kTcTileN * cg;
+                // measured on GB300: beyond ~6 stages (about 190 KB in flight) a deeper ring gains nothing
+                c.stages = std::min(6, max_stages(bm / cg, h->smem_optin));
+                c.split_k = split;
+                c.tail_split = 0;
+                if (check_tc_solution(h, p, c) != TL_SUCCESS) continue;
+                const double cost = tc_cost(h, p, c, in) * (split > 1 ? 1.0 + 0.02 * split : 1.0);
+                if (!have || cost < best * 0.995) {
+                    best = cost;
+                    *s = c;
+                    have = true;
+                }
+            }
+    if (!have) {
+        // nothing legal (the caller's check reports why): a plain one-SM tile
+        s->macro_tile0 = 128;
+        s->macro_tile1 = kTcTileN;
+        s->stages = std::min(6, max_stages(128, h->smem_optin));
+        s->split_k = 1;
+    }
+    s->wave_tile0 = 0;
+    s->wave_tile1 = 0;
     s->ctas = 0;
 }
 
@@ -620,16 +670,7 @@ std::vector<tl_gemm_solution> tc_candidates(const tl_handle* h, const tl_gemm_pr
                 if (is_split(kernel)) s.promote_k = 256;
                 if (raster && raster >= tiles_n) continue;
                 if (check_tc_solution(h, p, s) != TL_SUCCESS) continue;
-                // cost model: tensor work per tile grows with bm (efficiency of the 128 x bm MMA),
-                // waves quantise, split-k adds a partial round trip
-                const int64_t tiles = ((p.n + kTcTileN * cg - 1) / (kTcTileN * cg)) * ((p.m + bm - 1) / bm) * p.batch;
-                const int64_t work = tiles * split;
-                const double waves = std::ceil(static_cast<double>(work) / (h->sm_count / cg));
-                // per work unit: MMA time grows with the tile; a CTA pair stages half the n operand per SM
-                const double per_unit = (static_cast<double>(bm) / 256.0 + 0.15) * (cg == 2 ? 0.85 : 1.0) *
-                                        (static_cast<double>(num_kb) / split + 4.0);
-                double cost = waves * per_unit;
-                if (split > 1) cost *= 1.0 + 0.02 * split;
+                double cost = tc_cost(h, p, s, in) * (split > 1 ? 1.0 + 0.02 * split : 1.0);
                 if (raster == 0 && tiles_n > 8) cost *= 1.02;
                 ranked.push_back({cost, s});
             }
@@ -1012,11 +1053,19 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
         med.m = ms[count / 2];
         med.kernel = TL_KERNEL_TCGEN05;
         tc_heuristic(h, med, TL_KERNEL_TCGEN05, &s);
+        // a CTA pair per 256 x 256 tile (half the m-side operand per SM) where every problem allows it
         s.macro_tile0 = 256;
-        s.macro_tile1 = kTcTileN;
-        s.stages = max_stages(s.macro_tile0, h->smem_optin);
+        s.macro_tile1 = 2 * kTcTileN;
+        s.stages = std::min(6, max_stages(s.macro_tile0 / 2, h->smem_optin));
         s.split_k = 1;
         s.raster = 0;
+        s.tail_split = 0;
+        for (int i = 0; i < count; ++i)
+            if (check_tc_solution(h, probs[i], s) != TL_SUCCESS) {
+                s.macro_tile1 = kTcTileN;
+                s.stages = max_stages(s.macro_tile0, h->smem_optin);
+                break;
+            }
     }
     s.kernel = TL_KERNEL_TCGEN05;
     if (s.split_k == 0) s.split_k = 1;
@@ -1026,6 +1075,7 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
 
     std::vector<TcGroupEntry> host(count);
     std::vector<int64_t> prefix(count + 1, 0);
+    const int kb_elems = tl::kTcRowBytes / (p0.dtype_a == TL_DTYPE_FP8_E4M3 ? 1 : 2);
     double flops = 0;
     for (int i = 0; i < count; ++i) {
         const tl_gemm_problem& p = probs[i];
@@ -1053,17 +1103,30 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
         prefix[i + 1] = prefix[i] + static_cast<int64_t>(e.tiles_m) * e.tiles_n;
         flops += 2.0 * static_cast<double>(p.m) * p.n * p.k;
     }
+    // The unit table: work unit w -> (problem, tile row along n, tile column along m, k-blocks), in
+    // problem order, tiles of a problem n-major.  The kernel reads one 16-byte entry per tile
+    // (loaded a tile ahead) instead of searching the per-problem tile prefix.
+    const int64_t total_units = prefix[count];
+    if (total_units > INT32_MAX) return fail(TL_ERR_UNSUPPORTED, "grouped plan has too many tiles");
+    std::vector<int4> units(static_cast<size_t>(total_units));
+    for (int i = 0, w = 0; i < count; ++i) {
+        const TcGroupEntry& e = host[i];
+        const int nkb = static_cast<int>((e.K + kb_elems - 1) / kb_elems);
+        for (int in = 0; in < e.tiles_n; ++in)
+            for (int jm = 0; jm < e.tiles_m; ++jm) units[w++] = make_int4(i, in, jm, nkb);
+    }
     tl_grouped_plan* pl = new (std::nothrow) tl_grouped_plan();
     if (!pl) return fail(TL_ERR_ALLOC, "plan allocation failed");
     pl->h = h;
     cudaError_t e;
     if ((e = cudaMalloc(&pl->d_entries, sizeof(TcGroupEntry) * count)) != cudaSuccess ||
-        (e = cudaMalloc(&pl->d_prefix, sizeof(int64_t) * (count + 1))) != cudaSuccess) {
+        (total_units > 0 && (e = cudaMalloc(&pl->d_units, sizeof(int4) * units.size())) != cudaSuccess)) {
         tl_grouped_plan_destroy(pl);
         return cuda_fail(e, "cudaMalloc(plan)");
     }
     if ((e = cudaMemcpy(pl->d_entries, host.data(), sizeof(TcGroupEntry) * count, cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemcpy(pl->d_prefix, prefix.data(), sizeof(int64_t) * (count + 1), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        (total_units > 0 &&
+         (e = cudaMemcpy(pl->d_units, units.data(), sizeof(int4) * units.size(), cudaMemcpyHostToDevice)) != cudaSuccess)) {
         tl_grouped_plan_destroy(pl);
         return cuda_fail(e, "cudaMemcpy(plan)");
     }
@@ -1074,7 +1137,7 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
     G.n_mn_major = n_mn_major(p0) ? 1 : 0;
     G.m_mn_major = m_mn_major(p0) ? 1 : 0;
     G.d_entries = pl->d_entries;
-    G.d_tile_prefix = pl->d_prefix;
+    G.d_units = pl->d_units;
     G.count = count;
     G.total_tiles = prefix[count];
     G.bm = s.macro_tile0;
@@ -1103,9 +1166,9 @@ TL_API tl_status tl_grouped_plan_launch(tl_grouped_plan* pl, void* stream)
 TL_API tl_status tl_grouped_plan_destroy(tl_grouped_plan* pl)
 {
     if (!pl) return TL_SUCCESS;
-    if (pl->d_entries || pl->d_prefix) cudaDeviceSynchronize();
+    if (pl->d_entries || pl->d_units) cudaDeviceSynchronize();
     if (pl->d_entries) cudaFree(pl->d_entries);
-    if (pl->d_prefix) cudaFree(pl->d_prefix);
+    if (pl->d_units) cudaFree(pl->d_units);
     delete pl;
     return TL_SUCCESS;
 }

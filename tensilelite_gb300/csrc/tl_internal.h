@@ -108,7 +108,7 @@ struct TcGroupLaunch {
     int in_dtype, out_dtype, out_trunc;
     int n_mn_major, m_mn_major;
     const TcGroupEntry* d_entries;   // device
-    const int64_t* d_tile_prefix;    // device, count+1 entries
+    const int4* d_units;             // device, one entry per work unit: {problem, tile row, tile column, k-blocks}
     int count;
     int64_t total_tiles;
     int bm, stages, ctas;
