@@ -56,8 +56,9 @@ struct TcKernelParams {
                                   // k-blocks; the epilogue adds each chain into fp32 registers
     int tiles_m, tiles_n;
     int64_t total_work;
-    int64_t tail_start;           // work units below this are whole tiles; the rest split k
-    int tail_split;               // k splits of each tile from tail_start on
+    int64_t split_units;          // work units below this are k-slices of the first split_tiles tiles
+    int64_t split_tiles;          // tiles split along k (tail_split slices each); the rest are whole
+    int tail_split;               // k slices of each split tile
     int num_kb;
     int kb_elems;          // k elements per k-block (one 128-byte row)
     uint32_t idesc;
@@ -97,15 +98,15 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, cons
     if (p.group == nullptr) {
         int64_t tile;
         int split, nsplit;
-        if (w < p.tail_start) {
-            tile = w;
+        if (w < p.split_units) {
+            // split tiles come first, so the last arriver's reduction overlaps later whole tiles
+            tile = w / p.tail_split;
+            split = static_cast<int>(w % p.tail_split);
+            nsplit = p.tail_split;
+        } else {
+            tile = p.split_tiles + (w - p.split_units);
             split = 0;
             nsplit = 1;
-        } else {
-            const int64_t u = w - p.tail_start;
-            tile = p.tail_start + u / p.tail_split;
-            split = static_cast<int>(u % p.tail_split);
-            nsplit = p.tail_split;
         }
         const int64_t tpb = static_cast<int64_t>(p.tiles_m) * p.tiles_n;
         const int b = static_cast<int>(tile / tpb);
@@ -141,7 +142,7 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, cons
         j.split = split;
         j.nsplit = nsplit;
         j.tile = tile;
-        j.slot = tile - p.tail_start;
+        j.slot = tile;                 // split tiles are 0 .. split_tiles-1
     } else {
         // grouped: the unit's problem and tile come from the plan's unit table (loaded ahead by
         // the caller); only the epilogue reads the problem's entry
@@ -452,31 +453,52 @@ __device__ __forceinline__ void split_finish_tmem(const TcKernelParams& p, const
     const int is_last = *last_flag;
     if (is_last && ok) {
         __threadfence();
-        const int chunks = p.bm / 32;
+        // CPS 32-column chunks per step (two for 16-bit outputs, one for fp32, whose C takes twice
+        // the registers): their C values and every other split's partials are in flight together
+        // (the reduction is latency-bound), summed in split order
+        constexpr int CPS = sizeof(TD) == 4 ? 1 : 2;
+        const int chunks = p.bm / 32;     // even: bm is 64, 128, 192 or 256
         const size_t slab_elems = static_cast<size_t>(kTcTileN) * p.bm;
         const float* base = p.ws + static_cast<size_t>(j.slot) * j.nsplit * slab_elems + row;
-        for (int c = 0; c < chunks; ++c) {
-            float v[32];
+        for (int c = 0; c < chunks; c += CPS) {
+            const int m0 = j.m0 + c * 32;
+            uint32_t cw[CPS][32];
+            if (CPS > 1 && row_ok) {
 #pragma unroll
-            for (int i = 0; i < 32; ++i) v[i] = 0.f;
+                for (int q = 0; q < CPS; ++q) load_c_chunk<TD>(j, base_c, m0 + 32 * q, cw[q]);
+            }
+            float v[CPS * 32];
+#pragma unroll
+            for (int i = 0; i < CPS * 32; ++i) v[i] = 0.f;
             for (int s = 0; s < j.nsplit; ++s) {
                 if (s == j.split) {
-                    uint32_t r[32];
-                    __syncwarp();
-                    ptx::tmem_ld32(tbase + c * 32, r);
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) v[i] += __uint_as_float(r[i]);
+                    for (int q = 0; q < CPS; ++q) {
+                        uint32_t r[32];
+                        __syncwarp();
+                        ptx::tmem_ld32(tbase + (c + q) * 32, r);
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) v[32 * q + i] += __uint_as_float(r[i]);
+                    }
                 } else {
-                    float a[32];
+                    float a[CPS * 32];
                     const float* src = base + static_cast<size_t>(s) * slab_elems + static_cast<size_t>(c) * 32 * kTcTileN;
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) a[i] = __ldcg(src + i * kTcTileN);
+                    for (int i = 0; i < CPS * 32; ++i) a[i] = __ldcg(src + i * kTcTileN);
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) v[i] += a[i];
+                    for (int i = 0; i < CPS * 32; ++i) v[i] += a[i];
                 }
             }
-            const int m = j.m0 + c * 32;
-            if (row_ok && m < j.M) store_chunk<TD>(j, base_c, base_d, m, v, p.out_trunc);
+#pragma unroll
+            for (int q = 0; q < CPS; ++q) {
+                if (row_ok && m0 + 32 * q < j.M) {
+                    float o[32];
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) o[i] = v[32 * q + i];
+                    if constexpr (CPS > 1) store_chunk_pre<TD>(j, base_d, m0 + 32 * q, o, cw[q], p.out_trunc);
+                    else store_chunk<TD>(j, base_c, base_d, m0 + 32 * q, o, p.out_trunc);
+                }
+            }
         }
         if (et == 0) p.counters[j.slot] = 0;   // ready for the next launch
     }
@@ -1201,13 +1223,16 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     const size_t smem = tc_smem_bytes(L.bm / cg, L.stages);
     const int64_t tiles = static_cast<int64_t>(kp.tiles_m) * kp.tiles_n * L.batch;
     if (L.split_k > 1) {
-        kp.tail_start = 0;
+        kp.split_units = tiles * L.split_k;
+        kp.split_tiles = tiles;
         kp.tail_split = L.split_k;
         kp.total_work = tiles * L.split_k;
     } else {
-        // tail split: when the last wave of whole tiles would leave at least half of the persistent
-        // workers idle, split that wave's tiles along k so it finishes in a fraction of a wave
-        kp.tail_start = tiles;
+        // tail split: when a last wave of whole tiles would leave at least half of the persistent
+        // workers idle, that many tiles are split along k instead; their slices are scheduled
+        // first, so the partial-sum reductions overlap the whole tiles that follow
+        kp.split_units = 0;
+        kp.split_tiles = 0;
         kp.tail_split = 1;
         kp.total_work = tiles;
         const int workers = persistent_workers(L.in_dtype, L.out_dtype, cg, L.ctas, L.sm_count, smem);
@@ -1219,9 +1244,10 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
                 if (S > 8) S = 8;
                 const size_t need = static_cast<size_t>(rem) * cg * S * kTcTileN * L.bm * sizeof(float);
                 if (S >= 2 && static_cast<size_t>(rem) * cg <= L.counters_len && need <= L.workspace_bytes) {
-                    kp.tail_start = tiles - rem;
+                    kp.split_tiles = rem;
+                    kp.split_units = rem * S;
                     kp.tail_split = S;
-                    kp.total_work = kp.tail_start + rem * S;
+                    kp.total_work = rem * S + (tiles - rem);
                 }
             }
         }
@@ -1252,7 +1278,8 @@ tl_status tc_grouped_launch(const TcGroupLaunch& G, cudaStream_t stream, int64_t
     kp.split_k = 1;
     kp.nterms = 1;
     kp.total_work = G.total_tiles;
-    kp.tail_start = G.total_tiles;
+    kp.split_units = 0;
+    kp.split_tiles = 0;
     kp.tail_split = 1;
     kp.kb_elems = kTcRowBytes / dtype_bytes(G.in_dtype);
     kp.stride_c = 0;
