@@ -428,7 +428,8 @@ __device__ __forceinline__ void release_tmem(uint64_t* bar, int lane)
     ptx::tc_fence_before();
     __syncwarp();
     if (lane == 0) {
-        if constexpr (CG == 2) ptx::mbar_arrive_cluster(ptx::mapa_shared(ptx::smem_u32(bar), 0));
+        // the accumulator belongs to the pair's leader (the even rank of the pair)
+        if constexpr (CG == 2) ptx::mbar_arrive_cluster(ptx::mapa_shared(ptx::smem_u32(bar), ptx::cluster_ctarank() & ~1u));
         else ptx::mbar_arrive(bar);
     }
 }
@@ -506,15 +507,21 @@ __device__ __forceinline__ void split_finish_tmem(const TcKernelParams& p, const
     asm volatile("bar.sync 1, 128;" ::: "memory");   // last_flag is reused by the next tile
 }
 
-template <int KIND, typename TD, int CG>
+template <int KIND, typename TD, int CL>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_constant__ TcKernelParams p)
 {
-    // CG == 2: a cluster of two CTAs on two SMs works on one 256-row tile.  Each CTA stages its own
-    // 128 rows of the n-side operand and its half of the m-side operand; the leader (rank 0) issues
-    // the pair MMAs, whose accumulator rows 0-127 live in the leader's TMEM and 128-255 in the peer's.
-    // The leader arms its full barriers with both CTAs' bytes and both CTAs' TMA completions land on
-    // them; MMA completions are multicast to both CTAs, and both epilogues release the leader's TMEM
-    // buffers with remote arrivals.
+    // CL CTAs per cluster.  CL == 2: a CTA pair on two SMs works on one 256-row tile.  Each CTA
+    // stages its own 128 rows of the n-side operand and its half of the m-side operand; the leader
+    // (even rank) issues the pair MMAs, whose accumulator rows 0-127 live in the leader's TMEM and
+    // 128-255 in the peer's.  The leader arms its full barriers with both CTAs' bytes and both CTAs'
+    // TMA completions land on them; MMA completions are multicast to both CTAs, and both epilogues
+    // release the leader's TMEM buffers with remote arrivals.
+    // CL == 4: two such pairs on adjacent 256-row tiles with the same m range.  CTA r of one pair
+    // needs the same m-side rows as CTA r of the other, so each loads half of them and multicasts
+    // it to both (half the m-side L2 traffic); a ring slot is refilled only after both pairs' MMAs
+    // have released it (each slot's empty barrier expects one commit from each pair's leader).
+    constexpr int CG = CL >= 2 ? 2 : 1;         // CTAs per MMA (cta_group)
+    constexpr int MC = CL / CG;                 // pairs sharing the m-side operand
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const uint32_t bmc = static_cast<uint32_t>(p.bm) / CG;            // m-side rows staged by this CTA
@@ -532,10 +539,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
 
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    const uint32_t rank = (CG == 2) ? ptx::cluster_ctarank() : 0u;
-    const bool leader = (rank == 0);
-    const int64_t unit0 = (CG == 2) ? static_cast<int64_t>(ptx::cluster_id_x()) : static_cast<int64_t>(blockIdx.x);
-    const int64_t units = (CG == 2) ? static_cast<int64_t>(ptx::ncluster_x()) : static_cast<int64_t>(gridDim.x);
+    const uint32_t rank = (CL > 1) ? ptx::cluster_ctarank() : 0u;
+    const uint32_t pair_rank = rank & 1u;       // position within the CTA pair
+    const uint32_t pair_base = rank & ~1u;      // the pair's leader
+    const bool leader = (pair_rank == 0);
+    const int64_t unit0 = (CL > 1) ? static_cast<int64_t>(ptx::cluster_id_x()) : static_cast<int64_t>(blockIdx.x);
+    const int64_t units = (CL > 1) ? static_cast<int64_t>(ptx::ncluster_x()) : static_cast<int64_t>(gridDim.x);
     const bool promo = p.promote_kb > 0;
     const bool sep_small = promo && p.nterms > 1;
     // TMEM columns: main accumulator x2 (+ small-term accumulator x2 when they are kept apart)
@@ -546,7 +555,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
     if (threadIdx.x == 0) {
         for (int s = 0; s < p.stages; ++s) {
             ptx::mbar_init(&full[s], 1);
-            ptx::mbar_init(&empty[s], 1);
+            ptx::mbar_init(&empty[s], MC);
         }
         for (int a = 0; a < 2; ++a) {
             ptx::mbar_init(&tfull[a], 1);
@@ -576,7 +585,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
     }
     ptx::tc_fence_before();
     __syncthreads();
-    if constexpr (CG == 2) ptx::cluster_sync();     // peer barriers initialised before any remote arrive
+    if constexpr (CL > 1) ptx::cluster_sync();     // peer barriers initialised before any remote arrive
     ptx::tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
     // Launched as a programmatic dependent: everything above (barrier set-up, TMEM allocation,
@@ -590,9 +599,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
 
     if (warp == 0) {
         // ------------------------------------------------------------------ TMA producer (each CTA)
-        // One flat loop over (k-block, product) per tile; the bounded waits are single PTX blocks,
-        // so this single-lane loop has no data-dependent inner loop.
-        if (lane == 0) {
+        // One flat loop over (k-block, product) per tile, run by the whole warp in step: its waits
+        // (single PTX blocks, voted across the warp) and bookkeeping are warp-uniform, and one
+        // elected lane issues the copies.
+        {
             uint32_t stage = 0, phase = 0;
             constexpr int W = kTcRowBytes / (KIND == 0 ? 2 : 1);   // elements per 128-byte row
             const int n_mn = p.n_mn_major, m_mn = p.m_mn_major;
@@ -605,60 +615,74 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 TileJob j;
                 get_job(p, w, u, j);
                 const int n0 = j.n0 + static_cast<int>(rank) * kTcTileN;
-                const int m0 = j.m0 + static_cast<int>(rank * bmc);
+                const int m0 = j.m0 + static_cast<int>(pair_rank * bmc);
                 const int total = (j.kb1 - j.kb0) * nvirt;
                 int kb = j.kb0, v = 0;
                 for (int i = 0; i < total; ++i) {
-                    if (!ptx::mbar_wait(&empty[stage], phase ^ 1u, tlim)) {
-                        record_error(p, abort_flag, 1);
+                    if (!__all_sync(0xffffffffu, ptx::mbar_wait(&empty[stage], phase ^ 1u, tlim))) {
+                        if (lane == 0) record_error(p, abort_flag, 1);
                         ok = false;
                         break;
                     }
-                    uint8_t* sN = smem + static_cast<size_t>(stage) * stage_bytes;
-                    uint8_t* sM = sN + tileN_bytes;
-                    // split-precision products, smallest first (term table set by the host)
-                    const void* mapN = p.group ? j.tmN : static_cast<const void*>(&p.tmN[p.term_n[v]]);
-                    const void* mapM = p.group ? j.tmM : static_cast<const void*>(&p.tmM[p.term_m[v]]);
-                    const int k0 = kb * W;
-                    if constexpr (CG == 2) {
-                        // the leader arms its full barrier with both CTAs' bytes; the peer's loads
-                        // only complete transactions on it (they cannot run a phase ahead: the
-                        // peer refills a slot only after the leader's MMAs released it)
-                        const uint32_t fb = ptx::mapa_shared(ptx::smem_u32(&full[stage]), 0);
-                        if (leader) ptx::mbar_arrive_expect_tx(&full[stage], 2u * stage_bytes);
-                        if (!n_mn) {
-                            ptx::tma_load_3d_pair(sN, mapN, fb, k0, n0, j.b);
-                        } else {
+                    if (ptx::elect_one()) {
+                        uint8_t* sN = smem + static_cast<size_t>(stage) * stage_bytes;
+                        uint8_t* sM = sN + tileN_bytes;
+                        // split-precision products, smallest first (term table set by the host)
+                        const void* mapN = p.group ? j.tmN : static_cast<const void*>(&p.tmN[p.term_n[v]]);
+                        const void* mapM = p.group ? j.tmM : static_cast<const void*>(&p.tmM[p.term_m[v]]);
+                        const int k0 = kb * W;
+                        if constexpr (CG == 2) {
+                            // the leader arms its full barrier with both CTAs' bytes; the peer's loads
+                            // only complete transactions on it (they cannot run a phase ahead: the
+                            // peer refills a slot only after the leader's MMAs released it)
+                            const uint32_t fb = ptx::mapa_shared(ptx::smem_u32(&full[stage]), pair_base);
+                            if (leader) ptx::mbar_arrive_expect_tx(&full[stage], 2u * stage_bytes);
+                            if (!n_mn) {
+                                ptx::tma_load_3d_pair(sN, mapN, fb, k0, n0, j.b);
+                            } else {
 #pragma unroll
-                            for (int c = 0; c < kTcTileN / W; ++c)
-                                ptx::tma_load_3d_pair(sN + c * W * kTcRowBytes, mapN, fb, n0 + c * W, k0, j.b);
-                        }
-                        if (!m_mn) {
-                            ptx::tma_load_3d_pair(sM, mapM, fb, k0, m0, j.b);
-                        } else {
+                                for (int c = 0; c < kTcTileN / W; ++c)
+                                    ptx::tma_load_3d_pair(sN + c * W * kTcRowBytes, mapN, fb, n0 + c * W, k0, j.b);
+                            }
+                            if constexpr (MC == 2) {
+                                // this CTA's half of the m rows shared with CTA pair_rank of the other
+                                // pair; the copy lands in both and is counted on each pair's leader
+                                const int half = static_cast<int>(rank >> 1);
+                                const uint16_t mask = static_cast<uint16_t>((1u << pair_rank) | (1u << (pair_rank + 2)));
+                                if (!m_mn)
+                                    ptx::tma_load_3d_pair_mc(sM + half * (bmc / 2) * kTcRowBytes, mapM, fb, mask, k0,
+                                                             m0 + half * static_cast<int>(bmc / 2), j.b);
+                                else
+                                    ptx::tma_load_3d_pair_mc(sM + half * W * kTcRowBytes, mapM, fb, mask,
+                                                             m0 + half * W, k0, j.b);
+                            } else if (!m_mn) {
+                                ptx::tma_load_3d_pair(sM, mapM, fb, k0, m0, j.b);
+                            } else {
 #pragma unroll
-                            for (int c = 0; c < 4; ++c)      // bmc / W <= 4 chunks
-                                if (c * W < static_cast<int>(bmc))
-                                    ptx::tma_load_3d_pair(sM + c * W * kTcRowBytes, mapM, fb, m0 + c * W, k0, j.b);
-                        }
-                    } else {
-                        ptx::mbar_arrive_expect_tx(&full[stage], stage_bytes);
-                        if (!n_mn) {
-                            ptx::tma_load_3d(sN, mapN, &full[stage], k0, n0, j.b);
+                                for (int c = 0; c < 4; ++c)      // bmc / W <= 4 chunks
+                                    if (c * W < static_cast<int>(bmc))
+                                        ptx::tma_load_3d_pair(sM + c * W * kTcRowBytes, mapM, fb, m0 + c * W, k0, j.b);
+                            }
                         } else {
+                            ptx::mbar_arrive_expect_tx(&full[stage], stage_bytes);
+                            if (!n_mn) {
+                                ptx::tma_load_3d(sN, mapN, &full[stage], k0, n0, j.b);
+                            } else {
 #pragma unroll
-                            for (int c = 0; c < kTcTileN / W; ++c)
-                                ptx::tma_load_3d(sN + c * W * kTcRowBytes, mapN, &full[stage], n0 + c * W, k0, j.b);
-                        }
-                        if (!m_mn) {
-                            ptx::tma_load_3d(sM, mapM, &full[stage], k0, m0, j.b);
-                        } else {
+                                for (int c = 0; c < kTcTileN / W; ++c)
+                                    ptx::tma_load_3d(sN + c * W * kTcRowBytes, mapN, &full[stage], n0 + c * W, k0, j.b);
+                            }
+                            if (!m_mn) {
+                                ptx::tma_load_3d(sM, mapM, &full[stage], k0, m0, j.b);
+                            } else {
 #pragma unroll
-                            for (int c = 0; c < 4; ++c)      // bmc / W <= 4 chunks
-                                if (c * W < static_cast<int>(bmc))
-                                    ptx::tma_load_3d(sM + c * W * kTcRowBytes, mapM, &full[stage], m0 + c * W, k0, j.b);
+                                for (int c = 0; c < 4; ++c)      // bmc / W <= 4 chunks
+                                    if (c * W < static_cast<int>(bmc))
+                                        ptx::tma_load_3d(sM + c * W * kTcRowBytes, mapM, &full[stage], m0 + c * W, k0, j.b);
+                            }
                         }
                     }
+                    __syncwarp();
                     if (++stage == static_cast<uint32_t>(nstages)) {
                         stage = 0;
                         phase ^= 1u;
@@ -676,9 +700,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
         // alternate between tiles).  With promotion the A0*B0 product restarts its accumulation
         // every promote_kb k-blocks in the alternate buffer (the epilogue drains each chain into
         // fp32 registers), and the small split-precision products accumulate for the whole tile in
-        // a separate pair of buffers.  One flat loop per tile over (k-block, product).
-        if (lane == 0 && leader) {
+        // a separate pair of buffers.  One flat loop per tile over (k-block, product), run by the
+        // whole warp in step (uniform waits and bookkeeping); one elected lane issues the MMAs and
+        // their commits.
+        if (leader) {
             uint32_t stage = 0, phase = 0, mbuf = 0, mph = 0, sbuf = 0, sph = 0;
+            const uint16_t pair_mask = static_cast<uint16_t>(0x3u << pair_base);
             const uint32_t idesc = p.idesc;
             const uint32_t n_kstep = p.n_kstep, m_kstep = p.m_kstep, n_lbo = p.n_lbo, m_lbo = p.m_lbo;
             const uint32_t bmu = static_cast<uint32_t>(p.bm);
@@ -693,15 +720,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 const int nkb = j.kb1 - j.kb0;
                 const int chunk = promo ? p.promote_kb : (nkb > 0 ? nkb : 1);
                 if (sep_small) {
-                    if (!ptx::mbar_wait(&sempty[sbuf], sph ^ 1u, tlim)) {
-                        record_error(p, abort_flag, 2);
+                    if (!__all_sync(0xffffffffu, ptx::mbar_wait(&sempty[sbuf], sph ^ 1u, tlim))) {
+                        if (lane == 0) record_error(p, abort_flag, 2);
                         break;
                     }
                     ptx::tc_fence_after();
                 }
                 if (nkb > 0) {
-                    if (!ptx::mbar_wait(&tempty[mbuf], mph ^ 1u, tlim)) {
-                        record_error(p, abort_flag, 2);
+                    if (!__all_sync(0xffffffffu, ptx::mbar_wait(&tempty[mbuf], mph ^ 1u, tlim))) {
+                        if (lane == 0) record_error(p, abort_flag, 2);
                         break;
                     }
                     ptx::tc_fence_after();
@@ -710,8 +737,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 const int total = nkb * nvirt;
                 int v = 0, kb_in_chain = 0;
                 for (int i = 0; i < total; ++i) {
-                    if (!ptx::mbar_wait(&full[stage], phase, tlim)) {
-                        record_error(p, abort_flag, 4);
+                    if (!__all_sync(0xffffffffu, ptx::mbar_wait(&full[stage], phase, tlim))) {
+                        if (lane == 0) record_error(p, abort_flag, 4);
                         ok = false;
                         break;
                     }
@@ -721,23 +748,27 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                     const bool started = is_main ? main_started : small_started;
                     const uint32_t sN = ptx::smem_u32(smem + static_cast<size_t>(stage) * stage_bytes);
                     const uint32_t sM = sN + tileN_bytes;
+                    if (ptx::elect_one()) {
 #pragma unroll
-                    for (int ks = 0; ks < 4; ++ks) {
-                        const uint64_t adesc = ptx::sdesc_sw128(sN + ks * n_kstep, n_lbo, 1024);
-                        const uint64_t bdesc = ptx::sdesc_sw128(sM + ks * m_kstep, m_lbo, 1024);
-                        const uint32_t accumulate = (started || ks > 0) ? 1u : 0u;
-                        if constexpr (CG == 2) {
-                            if (KIND == 0) ptx::mma_f16_pair(d_tmem, adesc, bdesc, idesc, accumulate);
-                            else ptx::mma_f8_pair(d_tmem, adesc, bdesc, idesc, accumulate);
-                        } else {
-                            if (KIND == 0) ptx::mma_f16(d_tmem, adesc, bdesc, idesc, accumulate);
-                            else ptx::mma_f8(d_tmem, adesc, bdesc, idesc, accumulate);
+                        for (int ks = 0; ks < 4; ++ks) {
+                            const uint64_t adesc = ptx::sdesc_sw128(sN + ks * n_kstep, n_lbo, 1024);
+                            const uint64_t bdesc = ptx::sdesc_sw128(sM + ks * m_kstep, m_lbo, 1024);
+                            const uint32_t accumulate = (started || ks > 0) ? 1u : 0u;
+                            if constexpr (CG == 2) {
+                                if (KIND == 0) ptx::mma_f16_pair(d_tmem, adesc, bdesc, idesc, accumulate);
+                                else ptx::mma_f8_pair(d_tmem, adesc, bdesc, idesc, accumulate);
+                            } else {
+                                if (KIND == 0) ptx::mma_f16(d_tmem, adesc, bdesc, idesc, accumulate);
+                                else ptx::mma_f8(d_tmem, adesc, bdesc, idesc, accumulate);
+                            }
                         }
+                        // both pairs' ring slots are released (MC == 2: every CTA of the cluster)
+                        if constexpr (CG == 2) ptx::mma_commit_pair(&empty[stage], MC == 2 ? 0xF : 0x3);
+                        else ptx::mma_commit(&empty[stage]);
                     }
+                    __syncwarp();
                     main_started = main_started || is_main;
                     small_started = small_started || !is_main;
-                    if constexpr (CG == 2) ptx::mma_commit_pair(&empty[stage], 0x3);
-                    else ptx::mma_commit(&empty[stage]);
                     if (++stage == static_cast<uint32_t>(nstages)) {
                         stage = 0;
                         phase ^= 1u;
@@ -747,14 +778,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         // end of a chain of the main product: hand it to the epilogue, continue in
                         // the other buffer (a tile's last chain is handed over after the loop)
                         if (++kb_in_chain == chunk && i + 1 < total) {
-                            if constexpr (CG == 2) ptx::mma_commit_pair(&tfull[mbuf], 0x3);
-                            else ptx::mma_commit(&tfull[mbuf]);
+                            if (ptx::elect_one()) {
+                                if constexpr (CG == 2) ptx::mma_commit_pair(&tfull[mbuf], pair_mask);
+                                else ptx::mma_commit(&tfull[mbuf]);
+                            }
+                            __syncwarp();
                             mbuf ^= 1u;
                             if (mbuf == 0) mph ^= 1u;
                             kb_in_chain = 0;
                             main_started = false;
-                            if (!ptx::mbar_wait(&tempty[mbuf], mph ^ 1u, tlim)) {
-                                record_error(p, abort_flag, 2);
+                            if (!__all_sync(0xffffffffu, ptx::mbar_wait(&tempty[mbuf], mph ^ 1u, tlim))) {
+                                if (lane == 0) record_error(p, abort_flag, 2);
                                 ok = false;
                                 break;
                             }
@@ -763,15 +797,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                     }
                 }
                 if (!ok) break;
+                if (ptx::elect_one()) {
+                    if (nkb > 0) {
+                        if constexpr (CG == 2) ptx::mma_commit_pair(&tfull[mbuf], pair_mask);
+                        else ptx::mma_commit(&tfull[mbuf]);
+                    }
+                    if (sep_small) {
+                        if constexpr (CG == 2) ptx::mma_commit_pair(&sfull[sbuf], pair_mask);
+                        else ptx::mma_commit(&sfull[sbuf]);
+                    }
+                }
+                __syncwarp();
                 if (nkb > 0) {
-                    if constexpr (CG == 2) ptx::mma_commit_pair(&tfull[mbuf], 0x3);
-                    else ptx::mma_commit(&tfull[mbuf]);
                     mbuf ^= 1u;
                     if (mbuf == 0) mph ^= 1u;
                 }
                 if (sep_small) {
-                    if constexpr (CG == 2) ptx::mma_commit_pair(&sfull[sbuf], 0x3);
-                    else ptx::mma_commit(&sfull[sbuf]);
                     sbuf ^= 1u;
                     if (sbuf == 0) sph ^= 1u;
                 }
@@ -794,7 +835,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             TileJob j;
             get_job(p, w, u, j);
             j.n0 += static_cast<int>(rank) * kTcTileN;
-            j.slot = j.slot * CG + rank;              // split-k slabs and counters per CTA half
+            j.slot = j.slot * CL + rank;              // split-k slabs and counters per CTA
             const int n = j.n0 + row;
             const bool row_ok = n < j.N;
             const int64_t base_d = static_cast<int64_t>(j.b) * p.stride_d + static_cast<int64_t>(n) * j.ldd;
@@ -938,7 +979,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
 
     ptx::tc_fence_before();
     __syncthreads();
-    if constexpr (CG == 2) ptx::cluster_sync();     // no remote arrival or pair MMA still targets us
+    if constexpr (CL > 1) ptx::cluster_sync();     // no remote arrival, multicast or pair MMA still targets us
     if (warp == 1) {
         ptx::tc_fence_after();
         if constexpr (CG == 2) ptx::tmem_dealloc_pair(tmem_base, tmem_cols);
@@ -976,10 +1017,10 @@ bool pdl_enabled()
     return on;
 }
 
-template <int KIND, typename TD, int CG>
+template <int KIND, typename TD, int CL>
 tl_status launch_kernel(const TcKernelParams& kp, int grid, size_t smem, cudaStream_t stream)
 {
-    auto kern = tc_gemm_kernel<KIND, TD, CG>;
+    auto kern = tc_gemm_kernel<KIND, TD, CL>;
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;
     std::call_once(once, [&] {
@@ -1001,9 +1042,9 @@ tl_status launch_kernel(const TcKernelParams& kp, int grid, size_t smem, cudaStr
         attr[na].val.programmaticStreamSerializationAllowed = 1;
         ++na;
     }
-    if constexpr (CG == 2) {
+    if constexpr (CL > 1) {
         attr[na].id = cudaLaunchAttributeClusterDimension;
-        attr[na].val.clusterDim.x = 2;
+        attr[na].val.clusterDim.x = CL;
         attr[na].val.clusterDim.y = 1;
         attr[na].val.clusterDim.z = 1;
         ++na;
@@ -1011,32 +1052,32 @@ tl_status launch_kernel(const TcKernelParams& kp, int grid, size_t smem, cudaStr
     cfg.attrs = attr;
     cfg.numAttrs = na;
     cudaError_t e = cudaLaunchKernelEx(&cfg, kern, kp);
-    if (e != cudaSuccess) return cuda_fail(e, CG == 2 ? "cudaLaunchKernelEx(tc_gemm_kernel, cluster of 2)"
-                                                      : "cudaLaunchKernelEx(tc_gemm_kernel)");
+    if (e != cudaSuccess) return cuda_fail(e, CL > 1 ? "cudaLaunchKernelEx(tc_gemm_kernel, cluster launch)"
+                                                     : "cudaLaunchKernelEx(tc_gemm_kernel)");
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "tc_gemm_kernel launch");
     return TL_SUCCESS;
 }
 
-// Number of clusters of two that can be resident at once with this shared-memory size (cached).
-template <int KIND, typename TD>
-int max_pair_clusters(size_t smem)
+// Number of clusters of CL CTAs that can be resident at once with this shared-memory size (cached).
+template <int KIND, typename TD, int CL>
+int max_clusters(size_t smem)
 {
     static std::mutex mu;
     static std::map<size_t, int> cache;
     std::lock_guard<std::mutex> g(mu);
     auto it = cache.find(smem);
     if (it != cache.end()) return it->second;
-    auto kern = tc_gemm_kernel<KIND, TD, 2>;
+    auto kern = tc_gemm_kernel<KIND, TD, CL>;
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof(cfg));
-    cfg.gridDim = dim3(2, 1, 1);
+    cfg.gridDim = dim3(CL, 1, 1);
     cfg.blockDim = dim3(kTcThreads, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.x = CL;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
@@ -1050,49 +1091,54 @@ int max_pair_clusters(size_t smem)
     return n;
 }
 
-template <int CG>
-tl_status dispatch_cg(int in_dtype, int out_dtype, const TcKernelParams& kp, int grid, size_t smem, cudaStream_t s)
+template <int CL>
+tl_status dispatch_cl(int in_dtype, int out_dtype, const TcKernelParams& kp, int grid, size_t smem, cudaStream_t s)
 {
     const int kind = (in_dtype == TL_DTYPE_FP8_E4M3) ? 1 : 0;
     if (kind == 0) {
-        if (out_dtype == TL_DTYPE_FP32) return launch_kernel<0, float, CG>(kp, grid, smem, s);
-        if (out_dtype == TL_DTYPE_FP16) return launch_kernel<0, __half, CG>(kp, grid, smem, s);
-        if (out_dtype == TL_DTYPE_BF16) return launch_kernel<0, __nv_bfloat16, CG>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_FP32) return launch_kernel<0, float, CL>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_FP16) return launch_kernel<0, __half, CL>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_BF16) return launch_kernel<0, __nv_bfloat16, CL>(kp, grid, smem, s);
     } else {
-        if (out_dtype == TL_DTYPE_FP32) return launch_kernel<1, float, CG>(kp, grid, smem, s);
-        if (out_dtype == TL_DTYPE_FP16) return launch_kernel<1, __half, CG>(kp, grid, smem, s);
-        if (out_dtype == TL_DTYPE_BF16) return launch_kernel<1, __nv_bfloat16, CG>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_FP32) return launch_kernel<1, float, CL>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_FP16) return launch_kernel<1, __half, CL>(kp, grid, smem, s);
+        if (out_dtype == TL_DTYPE_BF16) return launch_kernel<1, __nv_bfloat16, CL>(kp, grid, smem, s);
     }
     return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel: unsupported output type");
 }
 
-// Persistent workers of a launch: CTAs (CG 1) or co-resident CTA pairs (CG 2).
-int persistent_workers(int in_dtype, int out_dtype, int cg, int ctas, int sm_count, size_t smem)
+template <int CL>
+int max_clusters_for(int in_dtype, int out_dtype, size_t smem)
 {
-    if (cg == 1) return ctas > 0 ? ctas : sm_count;
-    if (ctas > 0) return ctas / 2 > 0 ? ctas / 2 : 1;
-    const int kind = (in_dtype == TL_DTYPE_FP8_E4M3) ? 1 : 0;
-    int maxc = 0;
-    if (kind == 0)
-        maxc = out_dtype == TL_DTYPE_FP32   ? max_pair_clusters<0, float>(smem)
-               : out_dtype == TL_DTYPE_FP16 ? max_pair_clusters<0, __half>(smem)
-                                            : max_pair_clusters<0, __nv_bfloat16>(smem);
-    else
-        maxc = out_dtype == TL_DTYPE_FP32   ? max_pair_clusters<1, float>(smem)
-               : out_dtype == TL_DTYPE_FP16 ? max_pair_clusters<1, __half>(smem)
-                                            : max_pair_clusters<1, __nv_bfloat16>(smem);
-    return maxc > 0 ? maxc : sm_count / 2;
+    if (in_dtype != TL_DTYPE_FP8_E4M3)
+        return out_dtype == TL_DTYPE_FP32   ? max_clusters<0, float, CL>(smem)
+               : out_dtype == TL_DTYPE_FP16 ? max_clusters<0, __half, CL>(smem)
+                                            : max_clusters<0, __nv_bfloat16, CL>(smem);
+    return out_dtype == TL_DTYPE_FP32   ? max_clusters<1, float, CL>(smem)
+           : out_dtype == TL_DTYPE_FP16 ? max_clusters<1, __half, CL>(smem)
+                                        : max_clusters<1, __nv_bfloat16, CL>(smem);
 }
 
-// Grid: one CTA per SM (CG 1) or as many co-resident pairs as fit (CG 2), never more than the work.
-tl_status dispatch(int in_dtype, int out_dtype, int cg, const TcKernelParams& kp, int ctas, int sm_count,
+// Persistent workers of a launch: CTAs (cl 1) or co-resident clusters of cl CTAs (2: a CTA pair,
+// 4: two pairs sharing the m-side operand).
+int persistent_workers(int in_dtype, int out_dtype, int cl, int ctas, int sm_count, size_t smem)
+{
+    if (cl == 1) return ctas > 0 ? ctas : sm_count;
+    if (ctas > 0) return ctas / cl > 0 ? ctas / cl : 1;
+    const int maxc = cl == 2 ? max_clusters_for<2>(in_dtype, out_dtype, smem) : max_clusters_for<4>(in_dtype, out_dtype, smem);
+    return maxc > 0 ? maxc : sm_count / cl;
+}
+
+// Grid: one CTA per SM (cl 1) or as many co-resident clusters as fit, never more than the work.
+tl_status dispatch(int in_dtype, int out_dtype, int cl, const TcKernelParams& kp, int ctas, int sm_count,
                    int64_t total_work, size_t smem, cudaStream_t s)
 {
-    int workers = persistent_workers(in_dtype, out_dtype, cg, ctas, sm_count, smem);
+    int workers = persistent_workers(in_dtype, out_dtype, cl, ctas, sm_count, smem);
     if (workers > total_work) workers = static_cast<int>(total_work);
     if (workers < 1) workers = 1;
-    if (cg == 1) return dispatch_cg<1>(in_dtype, out_dtype, kp, workers, smem, s);
-    return dispatch_cg<2>(in_dtype, out_dtype, kp, 2 * workers, smem, s);
+    if (cl == 1) return dispatch_cl<1>(in_dtype, out_dtype, kp, workers, smem, s);
+    if (cl == 2) return dispatch_cl<2>(in_dtype, out_dtype, kp, 2 * workers, smem, s);
+    return dispatch_cl<4>(in_dtype, out_dtype, kp, 4 * workers, smem, s);
 }
 
 uint32_t make_idesc(int in_dtype, int n_mn_major, int m_mn_major, int bm, int cg)
@@ -1184,7 +1230,8 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     memset(&kp, 0, sizeof(kp));
     tl_status st;
     const int pieces = L.pieces < 1 ? 1 : L.pieces;
-    const int cg = L.cg == 2 ? 2 : 1;
+    const int cg = (L.cg == 2 || L.cg == 4) ? L.cg : 1;     // CTAs per cluster
+    const int cta_group = cg >= 2 ? 2 : 1;
     for (int i = 0; i < pieces; ++i) {
         if ((st = tc_encode_operand(&kp.tmN[i], L.in_dtype, L.opN[i], L.K, L.batch, kTcTileN)) != TL_SUCCESS) return st;
         if ((st = tc_encode_operand(&kp.tmM[i], L.in_dtype, L.opM[i], L.K, L.batch, L.bm / cg)) != TL_SUCCESS) return st;
@@ -1220,7 +1267,7 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     kp.num_kb = static_cast<int>((L.K + W - 1) / W);
     kp.kb_elems = W;
     kp.promote_kb = L.promote_k > 0 ? static_cast<int>((L.promote_k + W - 1) / W) : 0;
-    const size_t smem = tc_smem_bytes(L.bm / cg, L.stages);
+    const size_t smem = tc_smem_bytes(L.bm / cta_group, L.stages);
     const int64_t tiles = static_cast<int64_t>(kp.tiles_m) * kp.tiles_n * L.batch;
     if (L.split_k > 1) {
         kp.split_units = tiles * L.split_k;
@@ -1254,7 +1301,7 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     }
     kp.n_mn_major = L.opN[0].mn_major;
     kp.m_mn_major = L.opM[0].mn_major;
-    kp.idesc = make_idesc(L.in_dtype, kp.n_mn_major, kp.m_mn_major, L.bm, cg);
+    kp.idesc = make_idesc(L.in_dtype, kp.n_mn_major, kp.m_mn_major, L.bm, cta_group);
     desc_params(L.in_dtype, kp.n_mn_major, kp.n_lbo, kp.n_kstep);
     desc_params(L.in_dtype, kp.m_mn_major, kp.m_lbo, kp.m_kstep);
     kp.out_trunc = L.out_trunc;
@@ -1286,15 +1333,16 @@ tl_status tc_grouped_launch(const TcGroupLaunch& G, cudaStream_t stream, int64_t
     kp.stride_d = 0;
     kp.n_mn_major = G.n_mn_major;
     kp.m_mn_major = G.m_mn_major;
-    const int cg = G.cg == 2 ? 2 : 1;
+    const int cg = (G.cg == 2 || G.cg == 4) ? G.cg : 1;     // CTAs per cluster
+    const int cta_group = cg >= 2 ? 2 : 1;
     kp.tile_rows = kTcTileN * cg;
-    kp.idesc = make_idesc(G.in_dtype, G.n_mn_major, G.m_mn_major, G.bm, cg);
+    kp.idesc = make_idesc(G.in_dtype, G.n_mn_major, G.m_mn_major, G.bm, cta_group);
     desc_params(G.in_dtype, G.n_mn_major, kp.n_lbo, kp.n_kstep);
     desc_params(G.in_dtype, G.m_mn_major, kp.m_lbo, kp.m_kstep);
     kp.out_trunc = G.out_trunc;
     kp.err = G.err;
     kp.timeout_ns = G.timeout_ns;
-    const size_t smem = tc_smem_bytes(G.bm / cg, G.stages);
+    const size_t smem = tc_smem_bytes(G.bm / cta_group, G.stages);
     tl_status st = dispatch(G.in_dtype, G.out_dtype, cg, kp, G.ctas, G.sm_count, G.total_tiles, smem, stream);
     if (st == TL_SUCCESS && launches) ++*launches;
     return st;

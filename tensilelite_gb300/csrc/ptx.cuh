@@ -31,6 +31,18 @@ __device__ __forceinline__ void fence_mbar_init()
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+// One lane of a converged warp (elect.sync over the full mask); true in the elected lane only.
+__device__ __forceinline__ bool elect_one()
+{
+    uint32_t elected;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "elect.sync _|p, 0xffffffff;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(elected));
+    return elected != 0;
+}
+
 // Programmatic dependent launch: block until the prerequisite grid has completed and its memory
 // operations are visible (returns at once when the launch has no programmatic dependency).
 __device__ __forceinline__ void grid_dep_wait()
@@ -260,6 +272,17 @@ __device__ __forceinline__ void tma_load_3d_pair(void* smem_dst, const void* tma
         "cp.async.bulk.tensor.3d.cta_group::2.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
         " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(smem_dst)),
         "l"(reinterpret_cast<uint64_t>(tmap)), "r"(mbar_cluster_addr), "r"(x), "r"(y), "r"(z)
+        : "memory");
+}
+// The same load multicast to the CTAs in `cta_mask` (same shared-memory offset in each); each
+// destination's completion is counted on the mbarrier at the given offset in its own pair's leader.
+__device__ __forceinline__ void tma_load_3d_pair_mc(void* smem_dst, const void* tmap, uint32_t mbar_cluster_addr,
+                                                    uint16_t cta_mask, int x, int y, int z)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster"
+        ".cta_group::2 [%0], [%1, {%4, %5, %6}], [%2], %3;" ::"r"(smem_u32(smem_dst)),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(mbar_cluster_addr), "h"(cta_mask), "r"(x), "r"(y), "r"(z)
         : "memory");
 }
 // Collective over one warp in each CTA of the pair.

@@ -161,6 +161,17 @@ int resolve_kernel(const tl_gemm_problem& p)
     return p.dtype_a == TL_DTYPE_FP32 ? TL_KERNEL_SIMT : TL_KERNEL_TCGEN05;
 }
 
+// Two CTA pairs per cluster sharing the m-side operand (macro_tile1 512) as a heuristic/tuner choice:
+// on unless TL_CLUSTER4=0 in the environment (explicit solutions can always ask for it).
+bool cluster4_enabled()
+{
+    static const bool on = [] {
+        const char* e = getenv("TL_CLUSTER4");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 int max_stages(int bm_cta, size_t smem_optin)
 {
     int s = kTcMaxStages;
@@ -210,7 +221,8 @@ double tc_cost(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solut
         return std::max(mma_kb, bytes_kb / bw);
     };
     const int out_b = dtype_bytes(p.dtype_d);
-    const double epi = static_cast<double>(kTcTileN) * bm / cg * (out_b + (p.beta != 0.0f ? out_b : 0)) / 27.0;
+    // each CTA drains a 128 x bm accumulator (a pair's MMA is 256 x bm)
+    const double epi = static_cast<double>(kTcTileN) * bm * (out_b + (p.beta != 0.0f ? out_b : 0)) / 27.0;
     auto unit_time = [&](double kb, double active_ctas) { return std::max(kb * per_kb(active_ctas), epi) + 1500.0; };
     const double kb_unit = static_cast<double>(num_kb) / split;
     const int64_t full = units / workers, rem = units % workers;
@@ -260,14 +272,15 @@ void tc_heuristic(const tl_handle* h, const tl_gemm_problem& p, int kernel, tl_g
     double best = 0.0;
     bool have = false;
     tl_gemm_solution c = *s;
-    for (int cg : {2, 1})
+    for (int cg : {4, 2, 1})
         for (int bm : {256, 128, 192, 64})
             for (int split : {1, 2, 3, 4, 6, 8, 12, 16}) {
+                if (cg == 4 && !cluster4_enabled()) continue;
                 if (split > 1 && (split > num_kb / 2 || split > 16)) continue;
                 c.macro_tile0 = bm;
                 c.macro_tile1 = kTcTileN * cg;
                 // measured on GB300: beyond ~6 stages (about 190 KB in flight) a deeper ring gains nothing
-                c.stages = std::min(6, max_stages(bm / cg, h->smem_optin));
+                c.stages = std::min(6, max_stages(bm / (cg >= 2 ? 2 : 1), h->smem_optin));
                 c.split_k = split;
                 c.tail_split = 0;
                 if (check_tc_solution(h, p, c) != TL_SUCCESS) continue;
@@ -296,20 +309,27 @@ tl_status check_tc_solution(const tl_handle* h, const tl_gemm_problem& p, const 
     if (in != TL_DTYPE_FP16 && in != TL_DTYPE_BF16 && in != TL_DTYPE_FP8_E4M3)
         return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel needs fp16, bf16 or fp8 operands");
     const int W = row_elems(in);
-    if (s.macro_tile1 != kTcTileN && s.macro_tile1 != 2 * kTcTileN)
-        return fail(TL_ERR_UNSUPPORTED, "macro_tile1 (n) must be 128 (one SM) or 256 (a CTA pair) for tcgen05");
+    if (s.macro_tile1 != kTcTileN && s.macro_tile1 != 2 * kTcTileN && s.macro_tile1 != 4 * kTcTileN)
+        return fail(TL_ERR_UNSUPPORTED, "macro_tile1 (n) must be 128 (one SM), 256 (a CTA pair) or 512 (two pairs "
+                                        "sharing the m-side operand) for tcgen05");
     const int cg = s.macro_tile1 / kTcTileN;
+    const int cta_group = cg >= 2 ? 2 : 1;
     const int bm = s.macro_tile0;
     if (bm != 64 && bm != 128 && bm != 192 && bm != 256)
         return fail(TL_ERR_UNSUPPORTED, "macro_tile0 (m) must be 64, 128, 192 or 256");
     if (cg == 2 && bm != 128 && bm != 256)
         return fail(TL_ERR_UNSUPPORTED, "a CTA pair (macro_tile1 256) needs macro_tile0 128 or 256");
+    if (cg == 4 && (bm != 256 || s.promote_k > 0 || is_split(s.kernel)))
+        return fail(TL_ERR_UNSUPPORTED, "two CTA pairs (macro_tile1 512) need macro_tile0 256 and no promotion");
+    if (cg == 4 && m_mn_major(p) && bm / 2 != 2 * W)
+        return fail(TL_ERR_UNSUPPORTED, "two CTA pairs with MN-major A need two 128-byte chunks of m per CTA");
     const bool mmn = m_mn_major(p);
-    if (mmn && (bm / cg) % W)
+    if (mmn && (bm / cta_group) % W)
         return fail(TL_ERR_UNSUPPORTED, "m rows per CTA must be a multiple of the 128-byte row for MN-major A");
     if (s.depth_u != 0 && s.depth_u != W) return fail(TL_ERR_UNSUPPORTED, "depth_u is fixed to one 128-byte row");
     if (s.stages < 2 || s.stages > kTcMaxStages) return fail(TL_ERR_UNSUPPORTED, "stages must be in [2, 8]");
-    if (tc_smem_bytes(bm / cg, s.stages) > h->smem_optin) return fail(TL_ERR_UNSUPPORTED, "shared memory budget exceeded");
+    if (tc_smem_bytes(bm / cta_group, s.stages) > h->smem_optin)
+        return fail(TL_ERR_UNSUPPORTED, "shared memory budget exceeded");
     const int64_t num_kb = (p.k + W - 1) / W;
     if (s.split_k < 1 || (num_kb > 0 && s.split_k > num_kb) || s.split_k > 64)
         return fail(TL_ERR_UNSUPPORTED, "split_k must be in [1, min(64, k blocks)]");
@@ -653,9 +673,10 @@ std::vector<tl_gemm_solution> tc_candidates(const tl_handle* h, const tl_gemm_pr
     const int W = row_elems(in);
     const int64_t num_kb = std::max<int64_t>(1, (p.k + W - 1) / W);
     const int64_t tiles_n = (p.n + kTcTileN - 1) / kTcTileN;
-    for (int cg : {1, 2})
+    for (int cg : {1, 2, 4})
     for (int bm : {64, 128, 192, 256}) {
         for (int split : {1, 2, 3, 4, 6, 8, 12, 16}) {
+            if (cg == 4 && !cluster4_enabled()) continue;
             if (split > num_kb) continue;
             for (int raster : {0, 4, 8, 16}) {
                 tl_gemm_solution s;
@@ -664,7 +685,7 @@ std::vector<tl_gemm_solution> tc_candidates(const tl_handle* h, const tl_gemm_pr
                 s.macro_tile0 = bm;
                 s.macro_tile1 = kTcTileN * cg;
                 s.depth_u = W;
-                s.stages = max_stages(bm / cg, h->smem_optin);
+                s.stages = max_stages(bm / (cg >= 2 ? 2 : 1), h->smem_optin);
                 s.split_k = split;
                 s.raster = raster;
                 if (is_split(kernel)) s.promote_k = 256;
@@ -1210,15 +1231,16 @@ TL_API tl_status tl_tune_grouped(tl_handle* h, const tl_gemm_problem* probs, int
     cudaEventCreate(&e1);
     float best_t = 1e30f;
     bool any = false;
-    for (int cg : {1, 2})
+    for (int cg : {1, 2, 4})
     for (int bm : {64, 128, 192, 256}) {
         for (int stages : {3, 4, 6, 8}) {
+            if (cg == 4 && !cluster4_enabled()) continue;
             tl_gemm_solution c;
             memset(&c, 0, sizeof(c));
             c.kernel = TL_KERNEL_TCGEN05;
             c.macro_tile0 = bm;
             c.macro_tile1 = kTcTileN * cg;
-            c.stages = std::min(stages, max_stages(bm / cg, h->smem_optin));
+            c.stages = std::min(stages, max_stages(bm / (cg >= 2 ? 2 : 1), h->smem_optin));
             c.split_k = 1;
             if (stages > c.stages) continue;
             tl_grouped_plan* pl = nullptr;
