@@ -120,7 +120,9 @@ typedef struct tl_gemm_solution {
     int32_t raster;            /* tile rasterisation group width in tiles (0 = linear order) */
     int32_t ctas;              /* persistent CTAs (0 = one per SM) */
     int32_t promote_k;         /* k per tensor-core accumulation chain (0 = the whole k range) */
-    int32_t tail_split;        /* k splits of the tiles of a last, partial wave (0 auto, 1 off) */
+    int32_t tail_split;        /* split of a last, partial wave of tiles along k: 0 automatic,
+                                  1 off, S >= 2 each of its tiles in S equal k-slices, -1 its
+                                  k-blocks spread evenly over all workers (balanced) */
     int32_t reserved[4];
 } tl_gemm_solution;
 

@@ -27,6 +27,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -57,8 +58,14 @@ struct TcKernelParams {
     int tiles_m, tiles_n;
     int64_t total_work;
     int64_t split_units;          // work units below this are k-slices of the first split_tiles tiles
-    int64_t split_tiles;          // tiles split along k (tail_split slices each); the rest are whole
-    int tail_split;               // k slices of each split tile
+    int64_t split_tiles;          // tiles split along k; the rest are whole
+    int tail_split;               // k slices of each split tile (balanced: the workspace slab stride)
+    // balanced split (bal_kb > 0): the split tiles' bal_kb k-blocks are cut into bal_workers equal
+    // contiguous ranges, one per worker; unit w < 2 * bal_stride is piece w / bal_stride (a range
+    // spans at most two tiles) of worker w % bal_stride
+    int64_t bal_kb;
+    int bal_workers;
+    int bal_stride;
     int num_kb;
     int kb_elems;          // k elements per k-block (one 128-byte row)
     uint32_t idesc;
@@ -98,15 +105,47 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, cons
     if (p.group == nullptr) {
         int64_t tile;
         int split, nsplit;
-        if (w < p.split_units) {
+        int kb0, kb1;
+        if (p.bal_kb > 0 && w < 2 * static_cast<int64_t>(p.bal_stride)) {
+            // balanced split: worker `wk` owns k-blocks [s0, s1) of the split tiles laid end to end;
+            // piece 0 is the part in its first tile, piece 1 the rest (possibly empty)
+            const int64_t wk = w % p.bal_stride, piece = w / p.bal_stride;
+            const int64_t R = p.bal_kb, Wb = p.bal_workers, nkb = p.num_kb;
+            int64_t a = 0, e = 0;
+            if (wk < Wb) {
+                const int64_t s0 = wk * R / Wb, s1 = (wk + 1) * R / Wb;
+                const int64_t cut = min(s1, (s0 / nkb + 1) * nkb);
+                a = piece == 0 ? s0 : cut;
+                e = piece == 0 ? cut : s1;
+            }
+            if (a >= e) {
+                tile = 0;                    // empty unit: every role skips it
+                kb0 = kb1 = 0;
+                split = 0;
+                nsplit = 1;
+            } else {
+                tile = a / nkb;
+                kb0 = static_cast<int>(a - tile * nkb);
+                kb1 = static_cast<int>(e - tile * nkb);
+                // the workers covering this tile: the one holding its first and its last k-block
+                const int64_t first = ((tile * nkb + 1) * Wb - 1) / R;
+                const int64_t last = (((tile + 1) * nkb) * Wb - 1) / R;
+                nsplit = static_cast<int>(last - first + 1);
+                split = static_cast<int>(wk - first);
+            }
+        } else if (w < p.split_units) {
             // split tiles come first, so the last arriver's reduction overlaps later whole tiles
             tile = w / p.tail_split;
             split = static_cast<int>(w % p.tail_split);
             nsplit = p.tail_split;
+            kb0 = static_cast<int>((static_cast<int64_t>(split) * p.num_kb) / nsplit);
+            kb1 = static_cast<int>((static_cast<int64_t>(split + 1) * p.num_kb) / nsplit);
         } else {
             tile = p.split_tiles + (w - p.split_units);
             split = 0;
             nsplit = 1;
+            kb0 = 0;
+            kb1 = p.num_kb;
         }
         const int64_t tpb = static_cast<int64_t>(p.tiles_m) * p.tiles_n;
         const int b = static_cast<int>(tile / tpb);
@@ -137,8 +176,8 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, cons
         j.b = b;
         j.n0 = in * p.tile_rows;
         j.m0 = jm * p.bm;
-        j.kb0 = static_cast<int>((static_cast<int64_t>(split) * p.num_kb) / nsplit);
-        j.kb1 = static_cast<int>((static_cast<int64_t>(split + 1) * p.num_kb) / nsplit);
+        j.kb0 = kb0;
+        j.kb1 = kb1;
         j.split = split;
         j.nsplit = nsplit;
         j.tile = tile;
@@ -316,7 +355,7 @@ __device__ __forceinline__ void split_finish(const TcKernelParams& p, const Tile
 #pragma unroll
             for (int i = 0; i < 32; ++i) v[i] = 0.f;
             const size_t slab_elems = static_cast<size_t>(kTcTileN) * p.bm;
-            const float* src0 = p.ws + static_cast<size_t>(j.slot) * j.nsplit * slab_elems +
+            const float* src0 = p.ws + static_cast<size_t>(j.slot) * p.tail_split * slab_elems +
                                 static_cast<size_t>(c) * 32 * kTcTileN + row;
             for (int s = 0; s < j.nsplit; s += 2) {       // two slabs' loads in flight per step
                 float a[32], b[32];
@@ -460,7 +499,7 @@ __device__ __forceinline__ void split_finish_tmem(const TcKernelParams& p, const
         constexpr int CPS = sizeof(TD) == 4 ? 1 : 2;
         const int chunks = p.bm / 32;     // even: bm is 64, 128, 192 or 256
         const size_t slab_elems = static_cast<size_t>(kTcTileN) * p.bm;
-        const float* base = p.ws + static_cast<size_t>(j.slot) * j.nsplit * slab_elems + row;
+        const float* base = p.ws + static_cast<size_t>(j.slot) * p.tail_split * slab_elems + row;
         for (int c = 0; c < chunks; c += CPS) {
             const int m0 = j.m0 + c * 32;
             uint32_t cw[CPS][32];
@@ -718,7 +757,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 TileJob j;
                 get_job(p, w, u, j);
                 const int nkb = j.kb1 - j.kb0;
-                const int chunk = promo ? p.promote_kb : (nkb > 0 ? nkb : 1);
+                if (nkb <= 0) continue;                 // an empty unit of a balanced split
+                const int chunk = promo ? p.promote_kb : nkb;
                 if (sep_small) {
                     if (!__all_sync(0xffffffffu, ptx::mbar_wait(&sempty[sbuf], sph ^ 1u, tlim))) {
                         if (lane == 0) record_error(p, abort_flag, 2);
@@ -834,6 +874,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             const int4 u = load_unit(p, w);      // the epilogue trails the MMAs: no need to load ahead
             TileJob j;
             get_job(p, w, u, j);
+            if (j.kb1 <= j.kb0) continue;             // an empty unit of a balanced split
             j.n0 += static_cast<int>(rank) * kTcTileN;
             j.slot = j.slot * CL + rank;              // split-k slabs and counters per CTA
             const int n = j.n0 + row;
@@ -913,7 +954,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         }
                     }
                 } else {
-                    float* slab = p.ws + (static_cast<size_t>(j.slot) * j.nsplit + j.split) *
+                    float* slab = p.ws + (static_cast<size_t>(j.slot) * p.tail_split + j.split) *
                                              (static_cast<size_t>(kTcTileN) * p.bm);
                     if (ok) {
 #pragma unroll
@@ -959,7 +1000,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 }
             } else {
                 // split-k: park this split's partial tile, layout [chunk][column][row] (coalesced)
-                float* slab = p.ws + (static_cast<size_t>(j.slot) * j.nsplit + j.split) *
+                float* slab = p.ws + (static_cast<size_t>(j.slot) * p.tail_split + j.split) *
                                          (static_cast<size_t>(kTcTileN) * p.bm);
                 for (int c = 0; c < chunks && ok; ++c) {
                     uint32_t r[32];
@@ -1176,6 +1217,12 @@ size_t tc_smem_bytes(int bm, int stages)
     return static_cast<size_t>(stages) * (kTcTileN * kTcRowBytes + bm * kTcRowBytes) + 1024 + 512;
 }
 
+int tc_workers(int in_dtype, int out_dtype, int cl, int bm, int stages, int sm_count)
+{
+    const int cta_group = cl >= 2 ? 2 : 1;
+    return persistent_workers(in_dtype, out_dtype, cl, 0, sm_count, tc_smem_bytes(bm / cta_group, stages));
+}
+
 int tc_tmem_cols(int bm) { return (2 * bm <= 128) ? 128 : (2 * bm <= 256 ? 256 : 512); }
 
 tl_status tc_encode_operand(CUtensorMap* tm, int in_dtype, const TcOperand& op, int64_t K, int64_t batch,
@@ -1269,33 +1316,68 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     kp.promote_kb = L.promote_k > 0 ? static_cast<int>((L.promote_k + W - 1) / W) : 0;
     const size_t smem = tc_smem_bytes(L.bm / cta_group, L.stages);
     const int64_t tiles = static_cast<int64_t>(kp.tiles_m) * kp.tiles_n * L.batch;
+    kp.bal_kb = 0;
+    kp.bal_workers = 0;
+    kp.bal_stride = 0;
     if (L.split_k > 1) {
         kp.split_units = tiles * L.split_k;
         kp.split_tiles = tiles;
         kp.tail_split = L.split_k;
         kp.total_work = tiles * L.split_k;
     } else {
-        // tail split: when a last wave of whole tiles would leave at least half of the persistent
-        // workers idle, that many tiles are split along k instead; their slices are scheduled
-        // first, so the partial-sum reductions overlap the whole tiles that follow
         kp.split_units = 0;
         kp.split_tiles = 0;
         kp.tail_split = 1;
         kp.total_work = tiles;
         const int workers = persistent_workers(L.in_dtype, L.out_dtype, cg, L.ctas, L.sm_count, smem);
-        if (L.tail_split != 1 && L.workspace && tiles > workers) {
-            const int64_t rem = tiles % workers;
-            if (rem > 0 && 2 * rem <= workers) {
-                int S = L.tail_split > 1 ? L.tail_split : static_cast<int>(workers / rem);
-                if (S > kp.num_kb) S = kp.num_kb;
-                if (S > 8) S = 8;
-                const size_t need = static_cast<size_t>(rem) * cg * S * kTcTileN * L.bm * sizeof(float);
-                if (S >= 2 && static_cast<size_t>(rem) * cg <= L.counters_len && need <= L.workspace_bytes) {
-                    kp.split_tiles = rem;
-                    kp.split_units = rem * S;
-                    kp.tail_split = S;
-                    kp.total_work = rem * S + (tiles - rem);
-                }
+        const int64_t rem = tiles % workers, full = tiles / workers;
+        const size_t slab = static_cast<size_t>(kTcTileN) * L.bm * sizeof(float);
+        // measured on GB300: a piece needs about 48 k-blocks (balanced) or 16 (uniform slices) to
+        // amortise its partial-tile round trip; shorter pieces lose more than the idle workers
+        const int64_t R = rem * kp.num_kb;
+        const int64_t Wmax = std::min<int64_t>(std::min<int64_t>(workers, 8 * rem), R / 2);
+        // tail_split -1 asks for the balanced split whatever the piece length
+        const bool balanced = (L.tail_split == -1 || (L.tail_split == 0 && R / Wmax >= 48)) && L.promote_k == 0 &&
+                              Wmax >= rem && Wmax > 1;
+        if (balanced && L.workspace && rem > 0) {
+            // balanced split (automatic, long k): the k-blocks of the last partial wave's tiles
+            // are cut into equal contiguous ranges, one per worker (at most 8 pieces per tile); a
+            // range covers at most two tiles.  The pieces run first so their reductions overlap
+            // the whole tiles that follow; with no whole wave after them the reduction is exposed,
+            // so then the split must save a good part of a tile.
+            int64_t Wb = Wmax;
+            while (Wb >= rem) {
+                const int64_t per = R / Wb;
+                const int64_t maxS = (kp.num_kb + per - 1) / per + 1;
+                const size_t need = static_cast<size_t>(rem) * cg * maxS * slab;
+                if (need <= L.workspace_bytes && static_cast<size_t>(rem) * cg <= L.counters_len) break;
+                --Wb;
+            }
+            const int64_t saved = Wb >= rem ? kp.num_kb - (R + Wb - 1) / Wb : 0;
+            if (Wb >= rem && Wb > 1 &&
+                (L.tail_split == -1 || saved >= (full >= 1 ? 2 : std::max<int64_t>(8, kp.num_kb / 3)))) {
+                const int64_t per = R / Wb;
+                kp.bal_kb = R;
+                kp.bal_workers = static_cast<int>(Wb);
+                kp.bal_stride = workers;
+                kp.split_tiles = rem;
+                kp.split_units = 2 * static_cast<int64_t>(workers);
+                kp.tail_split = static_cast<int>((kp.num_kb + per - 1) / per + 1);   // slab stride
+                kp.total_work = 2 * static_cast<int64_t>(workers) + (tiles - rem);
+            }
+        } else if (L.tail_split != 1 && L.tail_split != -1 && L.workspace && tiles > workers && rem > 0 &&
+                   2 * rem <= workers) {
+            // uniform tail split (explicit S, or automatic): the last partial wave's tiles are cut
+            // into S equal k-slices, scheduled first
+            int S = L.tail_split > 1 ? L.tail_split : static_cast<int>(std::min<int64_t>(workers / rem, kp.num_kb / 16));
+            if (S > kp.num_kb) S = kp.num_kb;
+            if (S > 8) S = 8;
+            const size_t need = static_cast<size_t>(rem) * cg * S * slab;
+            if (S >= 2 && static_cast<size_t>(rem) * cg <= L.counters_len && need <= L.workspace_bytes) {
+                kp.split_tiles = rem;
+                kp.split_units = rem * S;
+                kp.tail_split = S;
+                kp.total_work = rem * S + (tiles - rem);
             }
         }
     }

@@ -211,7 +211,9 @@ double tc_cost(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solut
     const int bm = s.macro_tile0;
     const int64_t num_kb = std::max<int64_t>(1, (p.k + W - 1) / W);
     const int64_t tiles = ((p.n + kTcTileN * cg - 1) / (kTcTileN * cg)) * ((p.m + bm - 1) / bm) * p.batch;
-    const int64_t workers = std::max<int64_t>(1, h->sm_count / cg);
+    // real devices: the co-resident cluster count (clusters of 4 leave some SMs idle)
+    const int64_t workers = std::max<int64_t>(
+        1, h->d_err ? tc_workers(in_dtype, p.dtype_d, cg, bm, s.stages, h->sm_count) : h->sm_count / cg);
     const int64_t split = std::max<int64_t>(1, s.split_k);
     const int64_t units = tiles * split;
     const double mma_kb = std::max(656.0 * bm / 256.0, 300.0);
@@ -229,9 +231,17 @@ double tc_cost(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solut
     double cost = 6000.0 + epi;      // launch, prologue, the last tile's epilogue
     cost += static_cast<double>(full) * unit_time(kb_unit, static_cast<double>(std::min(units, workers)) * cg);
     if (rem > 0) {
-        if (split == 1 && s.tail_split != 1 && tiles > workers && 2 * rem <= workers) {
-            int64_t S = std::min<int64_t>(std::min<int64_t>(workers / rem, num_kb), 8);
-            if (s.tail_split > 1) S = std::min<int64_t>(s.tail_split, num_kb);
+        const int64_t R = rem * num_kb;
+        const int64_t Wb = std::min<int64_t>(std::min<int64_t>(workers, 8 * rem), R / 2);
+        int64_t S = std::min<int64_t>(std::min<int64_t>(workers / rem, num_kb / 16), 8);
+        if (s.tail_split > 1) S = std::min<int64_t>(s.tail_split, num_kb);
+        if (split == 1 && (s.tail_split == -1 || (s.tail_split == 0 && R / Wb >= 48)) && s.promote_k == 0 &&
+            Wb >= rem && Wb > 1) {
+            // balanced split of the last partial wave (reduction exposed without a whole wave after)
+            cost += unit_time(std::ceil(static_cast<double>(R) / Wb), static_cast<double>(workers * cg)) +
+                    (full >= 1 ? 1000.0 : 3000.0 + epi);
+        } else if (split == 1 && s.tail_split != 1 && s.tail_split != -1 && tiles > workers && 2 * rem <= workers &&
+                   S >= 2) {
             cost += unit_time(static_cast<double>(num_kb) / S, static_cast<double>(rem * S * cg)) + 2000.0 + epi;
         } else {
             cost += unit_time(kb_unit, static_cast<double>(rem * cg));
@@ -335,7 +345,7 @@ tl_status check_tc_solution(const tl_handle* h, const tl_gemm_problem& p, const 
         return fail(TL_ERR_UNSUPPORTED, "split_k must be in [1, min(64, k blocks)]");
     if (s.raster < 0 || s.ctas < 0) return fail(TL_ERR_INVALID_ARG, "raster and ctas must be >= 0");
     if (s.promote_k < 0) return fail(TL_ERR_INVALID_ARG, "promote_k must be >= 0");
-    if (s.tail_split < 0 || s.tail_split > 8) return fail(TL_ERR_INVALID_ARG, "tail_split must be in [0, 8]");
+    if (s.tail_split < -1 || s.tail_split > 8) return fail(TL_ERR_INVALID_ARG, "tail_split must be in [-1, 8]");
     if (s.promote_k > 0 && bm != 128)
         return fail(TL_ERR_UNSUPPORTED, "promote_k needs macro_tile0 == 128 (fp32 running sums, TMEM budget)");
     return TL_SUCCESS;
@@ -526,10 +536,12 @@ tl_status prepare(tl_handle* h, const tl_gemm_problem* prob, const tl_gemm_solut
         need = off_part + P.part_bytes;
         if ((st = ensure_counters(h, static_cast<size_t>(tiles))) != TL_SUCCESS) return st;
     } else if (P.s.tail_split != 1) {
-        // a split last wave uses at most one slab set per SM: split tiles x splits <= workers
+        // a split last wave: at most one tile per SM is split; an explicit tail split S keeps S
+        // partial slabs per tile, the automatic balanced split up to three (fewer, longer pieces
+        // are chosen at launch when a tile would need more)
         off_part = need;
         P.part_bytes = static_cast<size_t>(h->sm_count) * kTcTileN * P.s.macro_tile0 * sizeof(float) *
-                       static_cast<size_t>(P.s.tail_split > 1 ? P.s.tail_split : 1);
+                       static_cast<size_t>(P.s.tail_split > 1 ? P.s.tail_split : (P.s.tail_split == -1 ? 9 : 3));
         need = off_part + P.part_bytes;
         if ((st = ensure_counters(h, static_cast<size_t>(h->sm_count))) != TL_SUCCESS) return st;
     }

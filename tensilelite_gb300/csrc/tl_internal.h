@@ -95,6 +95,8 @@ struct TcLaunch {
 
 // Dynamic shared memory of one CTA staging bm_cta m-rows per stage (bm / 2 for a CTA pair).
 size_t tc_smem_bytes(int bm_cta, int stages);
+// Persistent workers (CTAs, or co-resident clusters of `cl` CTAs) a tensor-core launch gets.
+int tc_workers(int in_dtype, int out_dtype, int cl, int bm, int stages, int sm_count);
 int tc_tmem_cols(int bm);
 tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launches);
 // Checks a tcgen05 GEMM and fills its launch description without allocating anything; the caller

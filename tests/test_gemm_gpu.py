@@ -191,10 +191,11 @@ def test_grouped_cta_pair(h):
     plan.close()
 
 
-@pytest.mark.parametrize("cg,bm", [(1, 256), (2, 256), (1, 128)])
+@pytest.mark.parametrize("cg,bm", [(1, 256), (2, 256), (1, 128), (4, 256)])
 def test_tail_split_last_wave(h, cg, bm):
-    """More tiles than persistent workers with a small remainder: the last wave's tiles are split
-    along k (auto tail_split) and reduced through the workspace."""
+    """More tiles than persistent workers with a small remainder: the last wave's k-blocks are
+    spread evenly over all workers (auto tail_split: balanced pieces, one or two per worker) or its
+    tiles cut into 3 equal k-slices (tail_split 3), and reduced through the workspace."""
     m, n, k = 1024, 5120, 1024
     case = gg.make_case("bf16", "NN", 500 + cg + bm, m, n, k)
     sol = tl.Solution(kernel=tl.KERNEL_TCGEN05, macro_tile0=bm, macro_tile1=128 * cg, depth_u=64,
@@ -202,6 +203,20 @@ def test_tail_split_last_wave(h, cg, bm):
     check_case(h, case, "bf16", kernel="tcgen05", solution=sol)
     sol.tail_split = 3
     check_case(h, case, "bf16", kernel="tcgen05", solution=sol)
+    sol.tail_split = -1
+    check_case(h, case, "bf16", kernel="tcgen05", solution=sol)
+
+
+@pytest.mark.parametrize("cg,bm", [(1, 256), (2, 256), (4, 256), (2, 128)])
+@pytest.mark.parametrize("m,n,k", [(256, 512, 8192), (1000, 3008, 1344), (2048, 4608, 576)])
+def test_balanced_split_shapes(h, cg, bm, m, n, k):
+    """Balanced split of a partial wave at shapes where the pieces straddle tile boundaries, where
+    no whole wave follows (single partial wave, long k) and with ragged edges; C and beta on."""
+    case = gg.make_case("bf16", "NN", 900 + cg + bm + m % 97, m, n, k, alpha=0.75, beta=0.5, ld_align=8)
+    for tail in (0, -1):        # automatic, and the balanced split forced on
+        sol = tl.Solution(kernel=tl.KERNEL_TCGEN05, macro_tile0=bm, macro_tile1=128 * cg, depth_u=64,
+                          stages=4, split_k=1, tail_split=tail)
+        check_case(h, case, "bf16", kernel="tcgen05", solution=sol)
 
 
 def test_tc_fp32_output_and_truncation(h):
