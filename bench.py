@@ -487,6 +487,10 @@ def fp64_error(h, w, A, B, C, d, out_dt, scale_a, scale_b, base):
 
 
 def run_e2e(h, p, sol, base, dC, m, n, tdt, stream, steps, world):
+    """The GEMM through the public API with host buffers, pipelined over three streams: step i's
+    operands go host->device (tl_memcpy_h2d) while step i-1 computes (tl_gemm) and step i-2's result
+    goes device->host (tl_memcpy_d2h); device buffers are double-buffered and every hand-over is an
+    event, so each step still moves all of its inputs in and its whole result out."""
     import torch
     import tensilelite_gb300 as tl
     hA = torch.empty_like(base[0], device="cpu").pin_memory()
@@ -494,38 +498,57 @@ def run_e2e(h, p, sol, base, dC, m, n, tdt, stream, steps, world):
     hA.copy_(base[0].cpu())
     hB.copy_(base[1].cpu())
     hC = dC.cpu().pin_memory() if dC is not None else None
-    hD = torch.empty(m * n, dtype=tdt).pin_memory()
-    dA, dB = torch.empty_like(base[0]), torch.empty_like(base[1])
-    dC2 = torch.empty_like(dC) if dC is not None else None
-    dD = torch.empty(m * n, dtype=tdt, device="cuda")
+    hD = [torch.empty(m * n, dtype=tdt).pin_memory() for _ in range(2)]
+    dA = [torch.empty_like(base[0]) for _ in range(2)]
+    dB = [torch.empty_like(base[1]) for _ in range(2)]
+    dC2 = [torch.empty_like(dC) for _ in range(2)] if dC is not None else [None, None]
+    dD = [torch.empty(m * n, dtype=tdt, device="cuda") for _ in range(2)]
     L = tl.lib()
-    sp = stream.cuda_stream
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+    s_cmp = stream
+    ev_in = [torch.cuda.Event() for _ in range(2)]
+    ev_cmp = [torch.cuda.Event() for _ in range(2)]
+    ev_out = [torch.cuda.Event() for _ in range(2)]
     bi = hA.numel() * hA.element_size() + hB.numel() * hB.element_size() + (hC.numel() * hC.element_size() if hC is not None else 0)
-    bo = hD.numel() * hD.element_size()
+    bo = hD[0].numel() * hD[0].element_size()
+    used = [False, False]
 
-    def step():
-        tl.check(L.tl_memcpy_h2d(dA.data_ptr(), hA.data_ptr(), hA.numel() * hA.element_size(), sp))
-        tl.check(L.tl_memcpy_h2d(dB.data_ptr(), hB.data_ptr(), hB.numel() * hB.element_size(), sp))
+    def step(i):
+        b = i % 2
+        if used[b]:
+            s_in.wait_event(ev_cmp[b])        # the GEMM that read this input slot is done
+        tl.check(L.tl_memcpy_h2d(dA[b].data_ptr(), hA.data_ptr(), hA.numel() * hA.element_size(), s_in.cuda_stream))
+        tl.check(L.tl_memcpy_h2d(dB[b].data_ptr(), hB.data_ptr(), hB.numel() * hB.element_size(), s_in.cuda_stream))
         if hC is not None:
-            tl.check(L.tl_memcpy_h2d(dC2.data_ptr(), hC.data_ptr(), hC.numel() * hC.element_size(), sp))
-        h.gemm(p, dD, dC2, dA, dB, solution=sol, stream=stream)
-        tl.check(L.tl_memcpy_d2h(hD.data_ptr(), dD.data_ptr(), bo, sp))
+            tl.check(L.tl_memcpy_h2d(dC2[b].data_ptr(), hC.data_ptr(), hC.numel() * hC.element_size(), s_in.cuda_stream))
+        ev_in[b].record(s_in)
+        s_cmp.wait_event(ev_in[b])
+        if used[b]:
+            s_cmp.wait_event(ev_out[b])       # the result slot was read back
+        h.gemm(p, dD[b], dC2[b], dA[b], dB[b], solution=sol, stream=s_cmp)
+        ev_cmp[b].record(s_cmp)
+        s_out.wait_event(ev_cmp[b])
+        tl.check(L.tl_memcpy_d2h(hD[b].data_ptr(), dD[b].data_ptr(), bo, s_out.cuda_stream))
+        ev_out[b].record(s_out)
+        used[b] = True
 
-    for _ in range(3):
-        step()
-    stream.synchronize()
+    for i in range(4):
+        step(i)
+    torch.cuda.synchronize()
     barrier(world)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(steps):
-        step()
-    ev1.record(stream)
+    ev0.record(s_in)
+    for i in range(steps):
+        step(i)
+    s_in.wait_stream(s_out)
+    ev1.record(s_in)
     ev1.synchronize()
     ms = max_over_ranks(ev0.elapsed_time(ev1), world)
     flops = sum_over_ranks(p.flops() * steps, world)
     return {"value": round(flops / (ms / 1e3) / 1e12, 3), "unit": "TFLOP/s", "h2d_bytes_per_step": int(bi),
             "d2h_bytes_per_step": int(bo), "steps": steps, "ms_per_step": round(ms / steps, 4),
-            "path": "pinned host -> tl_memcpy_h2d -> tl_gemm -> tl_memcpy_d2h, one stream"}
+            "path": "pinned host -> tl_memcpy_h2d -> tl_gemm -> tl_memcpy_d2h, three streams pipelined "
+                    "(copies of step i+1 and i-1 overlap the GEMM of step i), double-buffered device operands"}
 
 
 def grouped_sizes(seed, count):
@@ -759,7 +782,8 @@ def run_fwdbwd(args, w, name):
                "path": "pinned host -> copy -> tensilelite_gb300.matmul fwd+bwd (eager) -> grads to pinned host"}
     clocks.stop()
     peaks = load_peaks()
-    achieved = flops / (kernel_ms_per_step / 1e3) / 1e12
+    # the replayed graph is the three GEMM kernels back to back: its time is their summed duration
+    achieved = value / max(world, 1)
     line = {"metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 6), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
@@ -773,8 +797,10 @@ def run_fwdbwd(args, w, name):
             "roofline": {"bound": "tensor", "achieved": round(achieved, 2), "peak": peaks["bf16_tflops"],
                          "unit": "TFLOP/s", "frac": round(achieved / peaks["bf16_tflops"], 4),
                          "traffic": None, "peak_source": peaks["source"] + " bf16 burst",
-                         "kernel_ms_per_step": round(kernel_ms_per_step, 6),
-                         "note": "achieved over the three GEMM kernels' summed event-timed durations"},
+                         "kernel_ms": round(ms / args.steps, 6),
+                         "eager_kernel_ms_per_step": round(kernel_ms_per_step, 6),
+                         "note": "achieved over the graph replay (the three GEMM kernels back to back); the eager "
+                                 "per-launch event pairs also time the host's launch gaps"},
             "accuracy_vs_fp64": err, "clocks": clocks.summary(mark0, mark1),
             "gpu_launches": int(round(eager_launches * args.steps))}
     if e2e:

@@ -267,7 +267,6 @@ void tc_heuristic(const tl_handle* h, const tl_gemm_problem& p, int kernel, tl_g
         // FP32-accurate paths: 128-wide tiles so the dominant product can be promoted out of TMEM
         // every 256 k (the chain length sets the tensor-core accumulation error)
         s->macro_tile0 = 128;
-        s->macro_tile1 = kTcTileN;
         s->promote_k = 256;
         const int64_t t128 = tiles_n * ((p.m + 127) / 128) * p.batch;
         int split = 1;
@@ -275,7 +274,13 @@ void tc_heuristic(const tl_handle* h, const tl_gemm_problem& p, int kernel, tl_g
             split = std::max(1, static_cast<int>(std::min<int64_t>(std::min<int64_t>(h->sm_count / std::max<int64_t>(1, t128),
                                                                                      num_kb / 4), 16)));
         s->split_k = split;
-        s->stages = std::min(6, max_stages(128, h->smem_optin));
+        // a CTA pair per 256 x 128 tile (half the m-side operand per SM): measured 6 % faster at 8192^3
+        s->macro_tile1 = 2 * kTcTileN;
+        s->stages = std::min(6, max_stages(64, h->smem_optin));
+        if (check_tc_solution(h, p, *s) != TL_SUCCESS) {
+            s->macro_tile1 = kTcTileN;
+            s->stages = std::min(6, max_stages(128, h->smem_optin));
+        }
         return;
     }
     // the legal tile with the least modelled time
