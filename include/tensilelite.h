@@ -170,6 +170,39 @@ TL_API tl_status tl_gemm(tl_handle* handle, const tl_gemm_problem* problem,
 TL_API tl_status tl_tune(tl_handle* handle, const tl_gemm_problem* problem, void* D, const void* C,
                          const void* A, const void* B, int max_candidates, int reps,
                          const char* cache_path, tl_gemm_solution* best, float* best_ms);
+/* ---- Tensile replacement-kernel entry ----------------------------------------------------------- */
+
+/* The argument buffer of the reference's Tensile-layout kernel (`-t 1`, src/gemmMfma.cpp:70-103;
+ * offsets by the kernel's argument table, src/gemmMfmaKernelWriter.h:321-338): 148 bytes, packed
+ * with natural alignment as below.  The kernel is Tensile's Cijk_Alik_Bljk (TN, column-major):
+ * D[i + j*stride_d0 + b*stride_d1] = alpha * sum_l A[l + i*stride_a0 + b*stride_a1] *
+ * B[l + j*stride_b0 + b*stride_b1] + beta * C[...], with i < sizes_free0, j < sizes_free1,
+ * b < sizes_free2, l < sizes_sum0.  alpha/beta are fp32 bits, or an fp16 value in the low half for
+ * the HBH kernel.  The launch-geometry fields (stagger, work-group counts, magic numbers) are
+ * Tensile's own and are ignored. */
+#define TL_TENSILE_KERNARG_BYTES 148
+typedef struct tl_tensile_kernarg {
+    uint64_t size_c, size_a, size_b;   /* elements of each buffer (0: unchecked) */
+    void* d;
+    const void* c;
+    const void* a;
+    const void* b;
+    uint32_t alpha_bits, beta_bits;
+    uint32_t stride_d0, stride_d1, stride_c0, stride_c1, stride_a0, stride_a1, stride_b0, stride_b1;
+    uint32_t sizes_free0, sizes_free1, sizes_free2, sizes_sum0;
+    uint32_t orig_stagger_u_iter, num_work_groups0, num_work_groups1, magic_number_problem_num_group_tiles0,
+        grid_num_work_groups0, num_full_blocks, wgm_remainder1, magic_number_wgm_remainder1, padding;
+} tl_tensile_kernarg;
+
+/* Run the GEMM a Tensile-layout kernel launch describes: `kernel_name` is
+ * Cijk_Alik_Bljk_{SB,HBH,BBH}[_...] (the names of src/gemmMfmaKernelWriter.h:376-378: fp32, fp16,
+ * bf16 operands and output; the bf16 output truncates as that kernel does), `kernarg` the argument
+ * buffer (at least TL_TENSILE_KERNARG_BYTES).  Asynchronous on `stream`, through tl_gemm with the
+ * handle's tuned or heuristic solution.  Replaces launching the generated kernel with Tensile's
+ * argument buffer (run_feifei_rpk.py:25-35 drives it from Tensile's client). */
+TL_API tl_status tl_tensile_launch(tl_handle* handle, const char* kernel_name, const void* kernarg,
+                                   size_t kernarg_bytes, void* stream);
+
 /* Load tuned solutions from a JSON file written by tl_tune into the handle's cache. */
 TL_API tl_status tl_load_solutions(tl_handle* handle, const char* cache_path, int* loaded);
 

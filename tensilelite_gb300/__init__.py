@@ -155,6 +155,7 @@ def lib():
         "tl_timer_elapsed_ms": [_vp, ctypes.POINTER(f32)], "tl_timer_destroy": [_vp],
         "tl_launch_count": [_vp, ctypes.POINTER(i64)], "tl_device_status": [_vp, _vp],
         "tl_set_kernel_timing": [_vp, i32],
+        "tl_tensile_launch": [_vp, ctypes.c_char_p, _vp, ctypes.c_size_t, _vp],
         "tl_kernel_timing": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(i64), i32],
         "tl_set_wait_timeout": [_vp, ctypes.c_uint32],
     }
@@ -170,6 +171,25 @@ def lib():
     L.tl_version.argtypes = []
     _LIB = L
     return L
+
+
+TENSILE_KERNARG_BYTES = 148
+
+
+def tensile_kernarg(D, C, A, B, m, n, k, *, batch=1, alpha=1.0, beta=0.0, half_scalars=False, stride_d0, stride_d1,
+                    stride_c0, stride_c1, stride_a0, stride_a1, stride_b0, stride_b1, size_c=0, size_a=0, size_b=0):
+    """Packs the reference's Tensile-layout argument buffer (148 bytes; tl_tensile_kernarg)."""
+    import struct
+    import numpy as np
+    if half_scalars:
+        ab = [int(np.array(x, np.float16).view(np.uint16)) for x in (alpha, beta)]
+    else:
+        ab = [int(np.array(x, np.float32).view(np.uint32)) for x in (alpha, beta)]
+    buf = struct.pack("<3Q4Q2I8I4I9I", size_c, size_a, size_b, _ptr(D) or 0, _ptr(C) or 0, _ptr(A) or 0,
+                      _ptr(B) or 0, ab[0], ab[1], stride_d0, stride_d1, stride_c0, stride_c1, stride_a0, stride_a1,
+                      stride_b0, stride_b1, m, n, batch, k, *([0] * 9))
+    assert len(buf) == TENSILE_KERNARG_BYTES
+    return buf
 
 
 def exported_symbols() -> list:
@@ -273,6 +293,12 @@ class Handle:
         n = ctypes.c_int64()
         check(lib().tl_launch_count(self._h, ctypes.byref(n)))
         return n.value
+
+    def tensile_launch(self, kernel_name: str, kernarg: bytes, stream=None):
+        """tl_tensile_launch: the GEMM a Tensile-layout (Cijk_Alik_Bljk) argument buffer describes."""
+        buf = ctypes.create_string_buffer(bytes(kernarg), len(kernarg))
+        check(lib().tl_tensile_launch(self._h, kernel_name.encode(), ctypes.cast(buf, _vp), len(kernarg),
+                                      _stream_ptr(stream)))
 
     def set_kernel_timing(self, enable: bool):
         """Record an event pair around every GEMM kernel launch (see tl_set_kernel_timing)."""

@@ -6,6 +6,7 @@
 // ff_gpu_src/ff_hip_runtime.cpp:278-320) and the runtime's buffer calls (inc/ff_gpu.h:240-333).
 // Unlike the reference, nothing here exits the process, launches are asynchronous on the caller's
 // stream, and the runtime is a per-device handle rather than a global singleton.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -962,6 +963,98 @@ TL_API tl_status tl_gemm(tl_handle* h, const tl_gemm_problem* p, const tl_gemm_s
     t_capturing = false;
     if (st != TL_SUCCESS) return st;
     return enqueue(h, P, S(stream));
+}
+
+// ---- Tensile-layout entry -------------------------------------------------------------------------
+// Fields of the packed argument buffer (no alignment assumed).
+static uint64_t karg_u64(const void* buf, size_t off)
+{
+    uint64_t v;
+    memcpy(&v, static_cast<const char*>(buf) + off, sizeof(v));
+    return v;
+}
+static uint32_t karg_u32(const void* buf, size_t off)
+{
+    uint32_t v;
+    memcpy(&v, static_cast<const char*>(buf) + off, sizeof(v));
+    return v;
+}
+static void* karg_ptr(const void* buf, size_t off)
+{
+    void* v;
+    memcpy(&v, static_cast<const char*>(buf) + off, sizeof(v));
+    return v;
+}
+
+// Last element touched by a TN operand or the output, +1 (elements): the extent to check against
+// the buffer size the caller declared.
+static uint64_t tn_extent(uint64_t rows, uint64_t cols, uint64_t ld, uint64_t batch, uint64_t batch_stride)
+{
+    if (rows == 0 || cols == 0 || batch == 0) return 0;
+    return (batch - 1) * batch_stride + (cols - 1) * ld + rows;
+}
+
+TL_API tl_status tl_tensile_launch(tl_handle* h, const char* kernel_name, const void* kernarg, size_t kernarg_bytes,
+                                   void* stream)
+{
+    if (!h || !kernel_name || !kernarg) return fail(TL_ERR_INVALID_ARG, "NULL argument");
+    if (kernarg_bytes < TL_TENSILE_KERNARG_BYTES)
+        return fail(TL_ERR_INVALID_ARG, "Tensile argument buffer shorter than 148 bytes");
+    const std::string name(kernel_name);
+    const std::string prefix = "Cijk_Alik_Bljk_";
+    if (name.compare(0, prefix.size(), prefix) != 0)
+        return fail(TL_ERR_UNSUPPORTED, "Tensile kernel " + name + ": only Cijk_Alik_Bljk (TN) is provided");
+    const std::string rest = name.substr(prefix.size());
+    auto is = [&](const char* tag) {
+        const size_t n = strlen(tag);
+        return rest.compare(0, n, tag) == 0 && (rest.size() == n || rest[n] == '_');
+    };
+    tl_dtype dt;
+    if (is("SB")) dt = TL_DTYPE_FP32;
+    else if (is("HBH")) dt = TL_DTYPE_FP16;
+    else if (is("BBH")) dt = TL_DTYPE_BF16;
+    else return fail(TL_ERR_UNSUPPORTED, "Tensile kernel " + name + ": data types must be SB, HBH or BBH");
+
+    const uint64_t size_c = karg_u64(kernarg, 0), size_a = karg_u64(kernarg, 8), size_b = karg_u64(kernarg, 16);
+    void* D = karg_ptr(kernarg, 24);
+    const void* C = karg_ptr(kernarg, 32);
+    const void* A = karg_ptr(kernarg, 40);
+    const void* B = karg_ptr(kernarg, 48);
+    const uint32_t alpha_bits = karg_u32(kernarg, 56), beta_bits = karg_u32(kernarg, 60);
+    uint32_t st[8];
+    for (int i = 0; i < 8; ++i) st[i] = karg_u32(kernarg, 64 + 4 * i);   // D0 D1 C0 C1 A0 A1 B0 B1
+    const uint32_t M = karg_u32(kernarg, 96), N = karg_u32(kernarg, 100), batch = karg_u32(kernarg, 104),
+                   K = karg_u32(kernarg, 108);
+    float alpha, beta;
+    if (dt == TL_DTYPE_FP16) {
+        // the HBH kernel takes alpha/beta as fp16 (converted in the kernel, src/gemmMfmaKernelWriter.h:1845-1854)
+        __half_raw ra, rb;
+        ra.x = static_cast<unsigned short>(alpha_bits & 0xFFFFu);
+        rb.x = static_cast<unsigned short>(beta_bits & 0xFFFFu);
+        alpha = __half2float(__half(ra));
+        beta = __half2float(__half(rb));
+    } else {
+        memcpy(&alpha, &alpha_bits, 4);
+        memcpy(&beta, &beta_bits, 4);
+    }
+    tl_gemm_problem p;
+    tl_status st0 = tl_problem_init(&p, dt, dt, TL_OP_T, TL_OP_N, M, N, K);
+    if (st0 != TL_SUCCESS) return st0;
+    p.batch = batch;
+    p.ldd = st[0]; p.stride_d = st[1];
+    p.ldc = st[2]; p.stride_c = st[3];
+    p.lda = st[4]; p.stride_a = st[5];
+    p.ldb = st[6]; p.stride_b = st[7];
+    p.alpha = alpha;
+    p.beta = beta;
+    if (dt == TL_DTYPE_BF16) p.out_rounding = TL_ROUND_TRUNCATE;   // the reference kernel's bf16 store
+    // the declared buffer sizes bound every access
+    if ((size_a && tn_extent(K, M, st[4], batch, st[5]) > size_a) ||
+        (size_b && tn_extent(K, N, st[6], batch, st[7]) > size_b) ||
+        (size_c && (tn_extent(M, N, st[0], batch, st[1]) > size_c ||
+                    (beta != 0.0f && tn_extent(M, N, st[2], batch, st[3]) > size_c))))
+        return fail(TL_ERR_INVALID_ARG, "Tensile arguments: strides and sizes exceed a declared buffer size");
+    return tl_gemm(h, &p, nullptr, D, C, A, B, stream);
 }
 
 TL_API tl_status tl_tune(tl_handle* h, const tl_gemm_problem* p, void* D, const void* C, const void* A,

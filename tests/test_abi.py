@@ -29,7 +29,7 @@ def test_no_undeclared_exports():
 
 
 def _c_sizeof(expr):
-    src = f'#include "include/tensilelite.h"\n#include <stdio.h>\n#include <stddef.h>\nint main(){{printf("%zu", {expr});}}'
+    src = f'#include "include/tensilelite.h"\n#include <stdio.h>\n#include <stddef.h>\nint main(){{printf("%zu", (size_t)({expr}));}}'
     exe = os.path.join("/tmp", "tl_sizeof_probe")
     r = subprocess.run(["gcc", "-x", "c", "-I", ROOT, "-o", exe, "-"], input=src, text=True, capture_output=True,
                        cwd=ROOT)
@@ -43,6 +43,42 @@ def test_struct_layout_matches_header():
     assert tl.Problem.alpha.offset == _c_sizeof("offsetof(tl_gemm_problem, alpha)")
     assert tl.Problem.out_rounding.offset == _c_sizeof("offsetof(tl_gemm_problem, out_rounding)")
     assert tl.Solution.ctas.offset == _c_sizeof("offsetof(tl_gemm_solution, ctas)")
+
+
+def test_tensile_kernarg_layout():
+    """tl_tensile_kernarg matches the reference's Tensile argument table (src/gemmMfmaKernelWriter.h:
+    321-338 with the 24-byte size prefix of src/gemmMfma.cpp:70-103): pointers at 24..56, alpha/beta
+    at 56/60, strides from 64, sizes from 96; 148 bytes used."""
+    offs = {"size_c": 0, "size_a": 8, "size_b": 16, "d": 24, "c": 32, "a": 40, "b": 48, "alpha_bits": 56,
+            "beta_bits": 60, "stride_d0": 64, "stride_d1": 68, "stride_c0": 72, "stride_c1": 76, "stride_a0": 80,
+            "stride_a1": 84, "stride_b0": 88, "stride_b1": 92, "sizes_free0": 96, "sizes_free1": 100,
+            "sizes_free2": 104, "sizes_sum0": 108, "padding": 144}
+    for field, off in offs.items():
+        assert _c_sizeof(f"offsetof(tl_tensile_kernarg, {field})") == off, field
+    assert _c_sizeof("TL_TENSILE_KERNARG_BYTES") == 148 == tl.TENSILE_KERNARG_BYTES
+    buf = tl.tensile_kernarg(0x1000, 0x2000, 0x3000, 0x4000, 96, 80, 64, batch=2, alpha=0.5, beta=0.25,
+                             stride_d0=160, stride_d1=12800, stride_c0=160, stride_c1=12800, stride_a0=128,
+                             stride_a1=12288, stride_b0=128, stride_b1=10240)
+    import struct
+    assert struct.unpack_from("<4Q", buf, 24) == (0x1000, 0x2000, 0x3000, 0x4000)
+    assert struct.unpack_from("<2f", buf, 56) == (0.5, 0.25)
+    assert struct.unpack_from("<4I", buf, 96) == (96, 80, 2, 64)
+
+
+def test_cli_help_lists_reference_options():
+    """The command-line runner takes the reference's options (inc/ff_utils.h:347-361); -h needs no GPU."""
+    import subprocess
+    cli = os.path.join(ROOT, "tensilelite_gb300", "tensilelite")
+    if not os.path.exists(cli):
+        pytest.skip("CLI not built")
+    out = subprocess.run([cli, "-h"], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0
+    for opt in ("-d --data-type", "-m --gemm-m", "-n --gemm-n", "-k --gemm-k", "-p --padding", "-r --mfma-pttn0",
+                "-s --mfma-pttn1", "-x --wave-pttn0", "-y --wave-pttn1", "-z --mfma-mn", "-u --depth-u",
+                "-v --verify", "-l --loop", "-f --buffer", "-t --tensile"):
+        assert opt in out.stdout, opt
+    bad = subprocess.run([cli, "-q", "1"], capture_output=True, text=True, timeout=60)
+    assert bad.returncode == 1 and "unknown" in bad.stderr
 
 
 def test_problem_init_defaults():

@@ -22,6 +22,7 @@ from tests.golden import gen_golden as gg
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 MANT = {"fp32": 23, "fp16": 10, "bf16": 7}
 
 
@@ -634,3 +635,74 @@ def test_autograd_layouts_match_fp64_gradient():
     for got, ref in ((Y, Xd @ Wd), (X.grad, dYd @ Wd.T), (W.grad, Xd.T @ dYd)):
         rel = float((got.double() - ref).abs().max() / ref.abs().max())
         assert rel < 1e-2
+
+
+# ---------------------------------------------------------------------------- Tensile layout, CLI
+@pytest.mark.parametrize("dt,name", [("fp32", "Cijk_Alik_Bljk_SB"), ("fp16", "Cijk_Alik_Bljk_HBH_MT64x64x16"),
+                                     ("bf16", "Cijk_Alik_Bljk_BBH")])
+def test_tensile_layout_launch_matches_gemm(h, dt, name):
+    """tl_tensile_launch decodes the reference's Tensile-layout argument buffer (padded TN problem,
+    batch 2) into the same GEMM tl_gemm runs: bit-equal outputs; bad names, short buffers and
+    declared sizes the strides overrun are refused."""
+    import torch
+    m, n, k, batch, pad = 192, 160, 256, 2, 64
+    lda = ldb = k + pad
+    ldc = ldd = m + pad
+    sa, sb, sc, sd = lda * m, ldb * n, ldc * n, ldd * n
+    tdt = {"fp32": torch.float32, "fp16": torch.float16, "bf16": torch.bfloat16}[dt]
+    gen = torch.Generator(device="cuda").manual_seed(61)
+    A = torch.randn(sa * batch, device="cuda", generator=gen).to(tdt)
+    B = torch.randn(sb * batch, device="cuda", generator=gen).to(tdt)
+    C = torch.randn(sc * batch, device="cuda", generator=gen).to(tdt)
+    D1 = torch.full((sd * batch,), float("nan"), device="cuda", dtype=tdt)
+    D2 = D1.clone()
+    alpha, beta = 0.314, 0.2718
+    if dt == "fp16":         # the HBH kernel takes fp16 scalars
+        alpha, beta = float(np.float16(alpha)), float(np.float16(beta))
+    p = tl.Problem.make(m, n, k, dtype=dt, trans_a=True, alpha=alpha, beta=beta, lda=lda, ldb=ldb, ldc=ldc, ldd=ldd,
+                        batch=batch, stride_a=sa, stride_b=sb, stride_c=sc, stride_d=sd,
+                        rounding="trunc" if dt == "bf16" else "rne")
+    h.gemm(p, D1, C, A, B)
+    kw = dict(batch=batch, alpha=alpha, beta=beta, half_scalars=dt == "fp16", stride_d0=ldd, stride_d1=sd,
+              stride_c0=ldc, stride_c1=sc, stride_a0=lda, stride_a1=sa, stride_b0=ldb, stride_b1=sb)
+    buf = tl.tensile_kernarg(D2, C, A, B, m, n, k, size_c=sc * batch, size_a=sa * batch, size_b=sb * batch, **kw)
+    h.tensile_launch(name, buf)
+    torch.cuda.synchronize()
+    h.device_status()
+    view = torch.int32 if dt == "fp32" else torch.int16
+    assert torch.equal(D1.view(view), D2.view(view))
+    with pytest.raises(tl.TLError) as e:
+        h.tensile_launch("Cijk_Ailk_Bljk_SB", buf)
+    assert e.value.status == tl.ERR_UNSUPPORTED
+    with pytest.raises(tl.TLError) as e:
+        h.tensile_launch(name, buf[:120])
+    assert e.value.status == tl.ERR_INVALID_ARG
+    small = tl.tensile_kernarg(D2, C, A, B, m, n, k, size_c=sc * batch, size_a=sa, size_b=sb * batch, **kw)
+    with pytest.raises(tl.TLError) as e:
+        h.tensile_launch(name, small)
+    assert e.value.status == tl.ERR_INVALID_ARG
+
+
+_CLI_CASES = [
+    ["-d", "1", "-m", "256", "-n", "192", "-k", "128", "-l", "3"],
+    ["-d", "2", "-m", "384", "-n", "256", "-k", "192", "-l", "3"],
+    ["-d", "3", "-m", "512", "-n", "512", "-k", "256", "-l", "3", "-z", "32", "-r", "4", "-x", "2", "-s", "4",
+     "-y", "1", "-f", "4"],
+    ["-d", "3", "-m", "256", "-n", "256", "-k", "128", "-l", "3", "-t", "1"],
+    ["--data-type", "2", "--gemm-m", "128", "--gemm-n", "128", "--gemm-k", "64", "--loop", "2", "-b", "2"],
+]
+
+
+@pytest.mark.parametrize("args", _CLI_CASES)
+def test_cli_runs_and_verifies(args):
+    """The command-line runner with the reference's options: runs, verifies against the CUDA-core
+    kernel (integer-pattern data, exact), prints the performance summary."""
+    import subprocess
+    cli = os.path.join(ROOT, "tensilelite_gb300", "tensilelite")
+    if not os.path.exists(cli):
+        pytest.skip("CLI not built")
+    out = subprocess.run([cli] + args, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "Performance =" in out.stdout
+    if "-t" not in args:
+        assert "Verify Success" in out.stdout, out.stdout
