@@ -42,6 +42,8 @@ namespace {
 
 struct TcKernelParams {
     CUtensorMap tmN[3], tmM[3];   // split-precision pieces 0..2 (piece 0 = the operand itself)
+    CUtensorMap tmD;              // the output, boxes of 128 bytes x 32 rows (tma_store)
+    int tma_store;                // whole tiles leave through shared memory and TMA stores
     const TcGroupEntry* group;
     const int4* group_units;       // per work unit: {problem, tile row, tile column, k-blocks}
     void* D;
@@ -416,6 +418,33 @@ __device__ __forceinline__ void load_c_chunk(const TileJob& j, int64_t base_c, i
     }
 }
 
+// alpha*acc + beta*C for 32 outputs (C in registers from load_c_chunk), converted and packed into
+// the output's bytes: 32 words for fp32, 16 for 16-bit types.
+template <typename TD>
+__device__ __forceinline__ void finish_pack(const TileJob& j, const uint32_t (&r)[32], const uint32_t (&cw)[32],
+                                            int trunc, uint32_t* out)
+{
+    const bool use_c = (j.beta != 0.0f) && (j.C != nullptr);
+    if constexpr (sizeof(TD) == 4) {
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+            const float a = __uint_as_float(r[i]);
+            out[i] = __float_as_uint(use_c ? fmaf(j.alpha, a, j.beta * __uint_as_float(cw[i])) : j.alpha * a);
+        }
+    } else {
+        constexpr int is_half = std::is_same<TD, __half>::value ? 1 : 0;
+#pragma unroll
+        for (int h = 0; h < 16; ++h) {
+            float c0 = 0.f, c1 = 0.f;
+            if (use_c) unpack2(cw[h], is_half, c0, c1);
+            const float a0 = __uint_as_float(r[2 * h]), a1 = __uint_as_float(r[2 * h + 1]);
+            const float o0 = use_c ? fmaf(j.alpha, a0, j.beta * c0) : j.alpha * a0;
+            const float o1 = use_c ? fmaf(j.alpha, a1, j.beta * c1) : j.alpha * a1;
+            out[h] = pack2(o0, o1, is_half, trunc);
+        }
+    }
+}
+
 // Finish a chunk with C already in registers (from load_c_chunk): v = alpha*acc + beta*C, store.
 template <typename TD>
 __device__ __forceinline__ void store_chunk_pre(const TileJob& j, int64_t base_d, int m, float (&acc)[32],
@@ -566,7 +595,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
     const uint32_t bmc = static_cast<uint32_t>(p.bm) / CG;            // m-side rows staged by this CTA
     const uint32_t tileN_bytes = kTcTileN * kTcRowBytes;
     const uint32_t stage_bytes = tileN_bytes + bmc * kTcRowBytes;
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(p.stages) * stage_bytes);
+    // output staging for TMA stores: 4 epilogue warps x 32 rows x 128 bytes, 1024-byte aligned
+    uint8_t* epi_stage = smem + static_cast<size_t>(p.stages) * stage_bytes;
+    uint64_t* full = reinterpret_cast<uint64_t*>(epi_stage + kTcEpiStageBytes);
     uint64_t* empty = full + kTcMaxStages;
     uint64_t* tfull = empty + kTcMaxStages;     // main accumulator buffers (per tile, or per chain)
     uint64_t* tempty = tfull + 2;
@@ -977,16 +1008,47 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             }
             const uint32_t tbase = tmem_base + lane_off + mbuf * static_cast<uint32_t>(p.bm);
             if (ok) ptx::tc_fence_after();
-            if (j.nsplit == 1) {
-                // C of chunk c+1 is loaded while chunk c is drained and stored
-                uint32_t cnext[32];
-                if (ok && row_ok) load_c_chunk<TD>(j, base_c, j.m0, cnext);
-                for (int c = 0; c < chunks && ok; ++c) {
-                    uint32_t ccur[32];
+            if (j.nsplit == 1 && p.tma_store) {
+                // each warp stages its 32 rows x 128 bytes of output (128-byte swizzle: 16-byte unit
+                // u of row r sits at u ^ (r & 7)) and writes them with one TMA store; the tensor
+                // map clips the ragged edges.  One staging buffer per warp: before refilling it the
+                // issuing lane waits until the previous store has read it.
+                constexpr int CPS = static_cast<int>(4 / sizeof(TD));    // 32-column chunks per 128 bytes
+                const uint32_t stg = ptx::smem_u32(epi_stage) + static_cast<uint32_t>(quarter) * 4096u;
+                const int nrow0 = j.n0 + quarter * 32;
+                for (int c0 = 0; c0 < chunks && ok; c0 += CPS) {
+                    const int m = j.m0 + c0 * 32;
+                    if (lane == 0) ptx::bulk_wait_read0();
+                    __syncwarp();
+                    const uint32_t rowaddr = stg + static_cast<uint32_t>(lane) * 128u;
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) ccur[i] = cnext[i];
+                    for (int q = 0; q < CPS; ++q) {
+                        uint32_t cw[32];
+                        if (row_ok) load_c_chunk<TD>(j, base_c, m + 32 * q, cw);
+                        uint32_t r[32];
+                        __syncwarp();
+                        ptx::tmem_ld32(tbase + (c0 + q) * 32, r);
+                        uint32_t w[32 / CPS];
+                        finish_pack<TD>(j, r, cw, p.out_trunc, w);
+#pragma unroll
+                        for (int uu = 0; uu < 8 / CPS; ++uu) {
+                            const int u = q * (8 / CPS) + uu;
+                            ptx::st_shared_v4(rowaddr + static_cast<uint32_t>((u ^ (lane & 7)) * 16), w[4 * uu],
+                                              w[4 * uu + 1], w[4 * uu + 2], w[4 * uu + 3]);
+                        }
+                    }
+                    if (c0 + CPS >= chunks) release_tmem<CG>(&tempty[mbuf], lane);
+                    ptx::fence_proxy_async_smem();
+                    __syncwarp();
+                    if (lane == 0 && m < j.M && nrow0 < j.N) {
+                        ptx::tma_store_3d(&p.tmD, epi_stage + quarter * 4096, m, nrow0, j.b);
+                        ptx::bulk_commit();
+                    }
+                }
+            } else if (j.nsplit == 1) {
+                // output TMA cannot address (unaligned D): 16-byte vector stores per thread
+                for (int c = 0; c < chunks && ok; ++c) {
                     const int m = j.m0 + c * 32;
-                    if (row_ok && c + 1 < chunks) load_c_chunk<TD>(j, base_c, m + 32, cnext);
                     uint32_t r[32];
                     __syncwarp();
                     ptx::tmem_ld32(tbase + c * 32, r);
@@ -995,7 +1057,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         float v[32];
 #pragma unroll
                         for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-                        store_chunk_pre<TD>(j, base_d, m, v, ccur, p.out_trunc);
+                        store_chunk<TD>(j, base_c, base_d, m, v, p.out_trunc);
                     }
                 }
             } else {
@@ -1018,6 +1080,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
         }
     }
 
+    if (warp >= 2 && lane == 0) ptx::bulk_wait0();   // the epilogue's TMA stores have completed
     ptx::tc_fence_before();
     __syncthreads();
     if constexpr (CL > 1) ptx::cluster_sync();     // no remote arrival, multicast or pair MMA still targets us
@@ -1046,6 +1109,16 @@ EncodeTiledFn get_encode_fn()
             fn = reinterpret_cast<EncodeTiledFn>(ptr);
     });
     return fn;
+}
+
+// TMA-store epilogue: on unless TL_TMA_STORE=0 in the environment.
+bool tma_store_enabled()
+{
+    static const bool on = [] {
+        const char* e = getenv("TL_TMA_STORE");
+        return !(e && e[0] == '0');
+    }();
+    return on;
 }
 
 // Programmatic dependent launch for the tensor-core kernel: on unless TL_PDL=0 in the environment.
@@ -1213,8 +1286,8 @@ void desc_params(int in_dtype, int mn_major, uint32_t& lbo, uint32_t& kstep)
 
 size_t tc_smem_bytes(int bm, int stages)
 {
-    // ring + 1024 bytes to align the ring + barriers/flags (with margin)
-    return static_cast<size_t>(stages) * (kTcTileN * kTcRowBytes + bm * kTcRowBytes) + 1024 + 512;
+    // ring + output staging + 1024 bytes to align the ring + barriers/flags (with margin)
+    return static_cast<size_t>(stages) * (kTcTileN * kTcRowBytes + bm * kTcRowBytes) + kTcEpiStageBytes + 1024 + 512;
 }
 
 int tc_workers(int in_dtype, int out_dtype, int cl, int bm, int stages, int sm_count)
@@ -1269,6 +1342,28 @@ tl_status tc_encode_operand(CUtensorMap* tm, int in_dtype, const TcOperand& op, 
         return fail(TL_ERR_INVALID_ARG, buf);
     }
     return TL_SUCCESS;
+}
+
+// Tensor map of the output for TMA stores: boxes of 128 bytes along m by 32 rows (n), 128-byte
+// swizzle.  False when TMA cannot address D (alignment of the base, ldd or batch stride).
+bool tc_encode_output(CUtensorMap* tm, int out_dtype, void* D, int64_t M, int64_t N, int64_t ldd, int64_t batch,
+                      int64_t stride_d)
+{
+    EncodeTiledFn enc = get_encode_fn();
+    if (!enc || !D) return false;
+    const int es = dtype_bytes(out_dtype);
+    if ((reinterpret_cast<uintptr_t>(D) & 15) || (ldd * es) % 16 || (batch > 1 && (stride_d * es) % 16)) return false;
+    const CUtensorMapDataType dt = out_dtype == TL_DTYPE_FP32   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                   : out_dtype == TL_DTYPE_FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                                : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    cuuint64_t dims[3] = {static_cast<cuuint64_t>(M), static_cast<cuuint64_t>(N), static_cast<cuuint64_t>(batch)};
+    cuuint64_t strides[2] = {static_cast<cuuint64_t>(ldd) * es,
+                             batch > 1 ? static_cast<cuuint64_t>(stride_d) * es
+                                       : ((static_cast<cuuint64_t>(ldd) * es * N) + 15) & ~cuuint64_t(15)};
+    cuuint32_t box[3] = {static_cast<cuuint32_t>(kTcRowBytes / es), 32, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    return enc(tm, dt, 3, D, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+               CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launches)
@@ -1387,6 +1482,11 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     desc_params(L.in_dtype, kp.n_mn_major, kp.n_lbo, kp.n_kstep);
     desc_params(L.in_dtype, kp.m_mn_major, kp.m_lbo, kp.m_kstep);
     kp.out_trunc = L.out_trunc;
+    // whole tiles leave through TMA stores (not with promotion, which drains chains into registers)
+    kp.tma_store = (L.promote_k == 0 && tma_store_enabled() &&
+                    tc_encode_output(&kp.tmD, L.out_dtype, L.D, L.M, L.N, L.ldd, L.batch, L.stride_d))
+                       ? 1
+                       : 0;
     kp.ws = L.workspace;
     kp.counters = L.counters;
     kp.err = L.err;

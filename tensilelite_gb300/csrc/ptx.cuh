@@ -285,6 +285,25 @@ __device__ __forceinline__ void tma_load_3d_pair_mc(void* smem_dst, const void* 
         "l"(reinterpret_cast<uint64_t>(tmap)), "r"(mbar_cluster_addr), "h"(cta_mask), "r"(x), "r"(y), "r"(z)
         : "memory");
 }
+// TMA store of one box from this CTA's shared memory (bulk async-group completion); elements
+// outside the tensor are not written.  Coordinates are non-negative; x * element size is a
+// multiple of 16 bytes.
+__device__ __forceinline__ void tma_store_3d(const void* tmap, const void* smem_src, int x, int y, int z)
+{
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+                     reinterpret_cast<uint64_t>(tmap)),
+                 "r"(smem_u32(smem_src)), "r"(x), "r"(y), "r"(z)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// Wait until the committed bulk stores of this thread have finished reading shared memory.
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// Wait until the committed bulk stores of this thread are complete.
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d)
+{
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
 // Collective over one warp in each CTA of the pair.
 __device__ __forceinline__ void tmem_alloc_pair(uint32_t* slot_smem, uint32_t ncols)
 {

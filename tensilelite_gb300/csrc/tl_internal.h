@@ -38,6 +38,7 @@ inline int dtype_bytes(int dt)
 constexpr int kTcMaxStages = 8;
 constexpr int kTcTileN = 128;          // tcgen05 M extent: problem n rows on TMEM lanes
 constexpr int kTcRowBytes = 128;       // one swizzle row: depth_u * element size
+constexpr int kTcEpiStageBytes = 4 * 32 * 128;   // output staging of the 4 epilogue warps (TMA stores)
 constexpr int kTcThreads = 192;        // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 
 // One operand's TMA view: K-major (rows x k, k contiguous) or MN-major (k rows of contiguous rows).
