@@ -44,6 +44,8 @@ struct TcKernelParams {
     CUtensorMap tmN[3], tmM[3];   // split-precision pieces 0..2 (piece 0 = the operand itself)
     CUtensorMap tmD;              // the output, boxes of 128 bytes x 32 rows (tma_store)
     int tma_store;                // whole tiles leave through shared memory and TMA stores
+    int par_reduce;               // every split unit runs in the first round: the splits of a tile
+                                  // wait for each other and reduce one share of it each
     const TcGroupEntry* group;
     const int4* group_units;       // per work unit: {problem, tile row, tile column, k-blocks}
     void* D;
@@ -575,6 +577,76 @@ __device__ __forceinline__ void split_finish_tmem(const TcKernelParams& p, const
     asm volatile("bar.sync 1, 128;" ::: "memory");   // last_flag is reused by the next tile
 }
 
+// Bounded wait until *ctr >= target (acquire at GPU scope); false once limit_ns has passed.
+__device__ __forceinline__ bool wait_counter_ge(const int* ctr, int target, uint64_t limit_ns)
+{
+    const uint64_t t0 = ptx::globaltimer();
+    while (true) {
+        int v;
+        asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+        if (v >= target) return true;
+        if (ptx::globaltimer() - t0 > limit_ns) return false;
+        __nanosleep(64);
+    }
+}
+
+// Split-k completion when every split unit of the launch is resident at once (all of them in the
+// first round of the persistent schedule): each split has parked its partial tile, waits until the
+// tile's other splits have too, then reduces its share of the tile -- 32-column chunks split,
+// split + nsplit, ... -- summing the partials in split order (the same sums, bit for bit, as the
+// last-arriver path) and runs their epilogue.  The tile counter counts arrivals up to nsplit, then
+// finished shares up to 2 * nsplit, when the last one resets it for the next launch.
+template <typename TD, int CG>
+__device__ __forceinline__ void split_finish_parallel(const TcKernelParams& p, const TileJob& j, bool& ok, int et,
+                                                      int lane, int row, bool row_ok, int64_t base_c, int64_t base_d,
+                                                      volatile int* last_flag, uint64_t* tempty_bar,
+                                                      volatile int* abort_flag)
+{
+    if (ok) release_tmem<CG>(tempty_bar, lane);     // this split's partial is in the workspace
+    __threadfence();
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    if (et == 0) {
+        int go = 0;
+        if (ok) {
+            atomicAdd(p.counters + j.slot, 1);
+            go = wait_counter_ge(p.counters + j.slot, j.nsplit, p.timeout_ns) ? 1 : 0;
+            if (!go) record_error(p, abort_flag, 16);
+        }
+        *last_flag = go;
+    }
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    const int go = *last_flag;
+    if (go) {
+        __threadfence();
+        const int chunks = p.bm / 32;
+        const size_t slab_elems = static_cast<size_t>(kTcTileN) * p.bm;
+        const float* base = p.ws + static_cast<size_t>(j.slot) * p.tail_split * slab_elems + row;
+        for (int c = j.split; c < chunks; c += j.nsplit) {
+            float v[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) v[i] = 0.f;
+            for (int s = 0; s < j.nsplit; ++s) {
+                float a[32];
+                const float* src = base + static_cast<size_t>(s) * slab_elems + static_cast<size_t>(c) * 32 * kTcTileN;
+#pragma unroll
+                for (int i = 0; i < 32; ++i) a[i] = __ldcg(src + i * kTcTileN);
+#pragma unroll
+                for (int i = 0; i < 32; ++i) v[i] += a[i];
+            }
+            const int m = j.m0 + c * 32;
+            if (row_ok && m < j.M) store_chunk<TD>(j, base_c, base_d, m, v, p.out_trunc);
+        }
+    } else {
+        ok = false;
+    }
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    if (et == 0 && go) {
+        __threadfence();
+        if (atomicAdd(p.counters + j.slot, 1) == 2 * j.nsplit - 1) atomicExch(p.counters + j.slot, 0);
+    }
+    asm volatile("bar.sync 1, 128;" ::: "memory");   // last_flag is reused by the next tile
+}
+
 template <int KIND, typename TD, int CL>
 __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_constant__ TcKernelParams p)
 {
@@ -1072,8 +1144,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
 #pragma unroll
                     for (int i = 0; i < 32; ++i) __stcg(dst + i * kTcTileN, __uint_as_float(r[i]));
                 }
-                split_finish_tmem<TD, CG>(p, j, ok, et, lane, row, row_ok, base_c, base_d, last_flag, tbase,
-                                          &tempty[mbuf]);
+                if (p.par_reduce)
+                    split_finish_parallel<TD, CG>(p, j, ok, et, lane, row, row_ok, base_c, base_d, last_flag,
+                                                  &tempty[mbuf], abort_flag);
+                else
+                    split_finish_tmem<TD, CG>(p, j, ok, et, lane, row, row_ok, base_c, base_d, last_flag, tbase,
+                                              &tempty[mbuf]);
             }
             mbuf ^= 1u;
             if (mbuf == 0) mph ^= 1u;
@@ -1109,6 +1185,16 @@ EncodeTiledFn get_encode_fn()
             fn = reinterpret_cast<EncodeTiledFn>(ptr);
     });
     return fn;
+}
+
+// Parallel split-k reduction: on unless TL_PAR_REDUCE=0 in the environment.
+bool par_reduce_enabled()
+{
+    static const bool on = [] {
+        const char* e = getenv("TL_PAR_REDUCE");
+        return !(e && e[0] == '0');
+    }();
+    return on;
 }
 
 // TMA-store epilogue: on unless TL_TMA_STORE=0 in the environment.
@@ -1482,6 +1568,11 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     desc_params(L.in_dtype, kp.n_mn_major, kp.n_lbo, kp.n_kstep);
     desc_params(L.in_dtype, kp.m_mn_major, kp.m_lbo, kp.m_kstep);
     kp.out_trunc = L.out_trunc;
+    // all split units in the first round of the persistent schedule: parallel reduction
+    {
+        const int workers = persistent_workers(L.in_dtype, L.out_dtype, cg, L.ctas, L.sm_count, smem);
+        kp.par_reduce = (kp.split_units > 0 && kp.bal_kb == 0 && kp.split_units <= workers && par_reduce_enabled()) ? 1 : 0;
+    }
     // whole tiles leave through TMA stores (not with promotion, which drains chains into registers)
     kp.tma_store = (L.promote_k == 0 && tma_store_enabled() &&
                     tc_encode_output(&kp.tmD, L.out_dtype, L.D, L.M, L.N, L.ldd, L.batch, L.stride_d))

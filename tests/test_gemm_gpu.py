@@ -208,6 +208,18 @@ def test_tail_split_last_wave(h, cg, bm):
     check_case(h, case, "bf16", kernel="tcgen05", solution=sol)
 
 
+@pytest.mark.parametrize("cg,bm,split", [(1, 128, 3), (2, 256, 2), (1, 64, 4)])
+def test_split_k_reductions(h, cg, bm, split):
+    """Explicit split-k with few units (all resident: the splits of a tile reduce one share each in
+    parallel) and with many (more units than workers: the last split to arrive reduces the tile);
+    both sum in split order."""
+    for (m, n, k) in ((480, 1024, 2048), (2048, 2048, 512)):
+        case = gg.make_case("bf16", "NN", 700 + cg + bm + split + m % 7, m, n, k, alpha=1.25, beta=0.5)
+        sol = tl.Solution(kernel=tl.KERNEL_TCGEN05, macro_tile0=bm, macro_tile1=128 * cg, depth_u=64,
+                          stages=4, split_k=split)
+        check_case(h, case, "bf16", kernel="tcgen05", solution=sol)
+
+
 @pytest.mark.parametrize("cg,bm", [(1, 256), (2, 256), (4, 256), (2, 128)])
 @pytest.mark.parametrize("m,n,k", [(256, 512, 8192), (1000, 3008, 1344), (2048, 4608, 576)])
 def test_balanced_split_shapes(h, cg, bm, m, n, k):
