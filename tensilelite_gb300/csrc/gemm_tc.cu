@@ -85,6 +85,7 @@ struct TcKernelParams {
 struct TileJob {
     const void* tmN;
     const void* tmM;
+    const CUtensorMap* tmD;       // the output for TMA stores, or null
     void* D;
     const void* C;
     int64_t ldd, ldc;
@@ -169,6 +170,7 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, cons
         }
         j.tmN = &p.tmN[0];
         j.tmM = &p.tmM[0];
+        j.tmD = p.tma_store ? &p.tmD : nullptr;
         j.D = static_cast<char*>(p.D);
         j.C = p.C;
         j.ldd = p.ldd;
@@ -192,6 +194,7 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, cons
         const TcGroupEntry& e = p.group[u.x];
         j.tmN = &e.tmN;
         j.tmM = &e.tmM;
+        j.tmD = e.tma_store ? &e.tmD : nullptr;
         j.D = e.D;
         j.C = e.C;
         j.ldd = e.ldd;
@@ -1080,7 +1083,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             }
             const uint32_t tbase = tmem_base + lane_off + mbuf * static_cast<uint32_t>(p.bm);
             if (ok) ptx::tc_fence_after();
-            if (j.nsplit == 1 && p.tma_store) {
+            if (j.nsplit == 1 && j.tmD != nullptr) {
                 // each warp stages its 32 rows x 128 bytes of output (128-byte swizzle: 16-byte unit
                 // u of row r sits at u ^ (r & 7)) and writes them with one TMA store; the tensor
                 // map clips the ragged edges.  One staging buffer per warp: before refilling it the
@@ -1113,7 +1116,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                     ptx::fence_proxy_async_smem();
                     __syncwarp();
                     if (lane == 0 && m < j.M && nrow0 < j.N) {
-                        ptx::tma_store_3d(&p.tmD, epi_stage + quarter * 4096, m, nrow0, j.b);
+                        ptx::tma_store_3d(j.tmD, epi_stage + quarter * 4096, m, nrow0, j.b);
                         ptx::bulk_commit();
                     }
                 }

@@ -198,11 +198,9 @@ bool n_mn_major(const tl_gemm_problem& p) { return p.trans_b == TL_OP_T; }   // 
 
 tl_status check_tc_solution(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solution& s);
 
-// Modelled duration of one tensor-core launch, in SM clocks.  Per 128-byte k-block a CTA needs the
-// larger of its MMA time (656 clocks for a 128 x 256 x 64 bf16 block, proportional to the tile
-// width, floor 300) and its operand bytes over the L2-to-SM bandwidth (about 38 bytes per clock per
-// SM with every SM loading, more when fewer do) -- measured on GB300, the second term decides most
-// shapes, which is why a CTA pair (half the m-side operand per SM) wins even on a partial wave.
+// Modelled duration of one tensor-core launch, in SM clocks.  Per 128-byte k-block a CTA needs its
+// MMA issue time plus a cost per operand byte it stages (below) -- so a CTA pair or two pairs
+// sharing the m-side operand (fewer bytes per SM) win even on a partial wave.
 // Tiles run in persistent waves; a last wave that would leave half the workers idle is split along
 // k as the launch does; a tile's epilogue overlaps the next tile's main loop unless it is longer.
 double tc_cost(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solution& s, int in_dtype)
@@ -217,11 +215,15 @@ double tc_cost(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solut
         1, h->d_err ? tc_workers(in_dtype, p.dtype_d, cg, bm, s.stages, h->sm_count) : h->sm_count / cg);
     const int64_t split = std::max<int64_t>(1, s.split_k);
     const int64_t units = tiles * split;
-    const double mma_kb = std::max(656.0 * bm / 256.0, 300.0);
+    // per k-block and CTA: the MMA issue time (4 MMAs; about 500 clocks for any width up to 128
+    // columns, 716 for 256) plus a cost per staged operand byte that grows with the number of SMs
+    // loading at once -- fitted to the per-k-block times measured on GB300 for one SM / a pair,
+    // 128 / 256 columns (690-1000 clocks with every SM busy)
+    const double mma_kb = std::max(716.0 * bm / 256.0, 500.0);
     const double bytes_kb = static_cast<double>(kTcTileN) * kTcRowBytes + static_cast<double>(bm) / cg * kTcRowBytes;
     auto per_kb = [&](double active_ctas) {
-        const double bw = std::min(64.0, 38.0 * h->sm_count / std::max(1.0, active_ctas));
-        return std::max(mma_kb, bytes_kb / bw);
+        const double load = std::max(0.5, std::min(1.0, active_ctas / h->sm_count));
+        return mma_kb + bytes_kb * 0.0068 * load;
     };
     const int out_b = dtype_bytes(p.dtype_d);
     // each CTA drains a 128 x bm accumulator (a pair's MMA is 256 x bm)
@@ -248,7 +250,13 @@ double tc_cost(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solut
             cost += unit_time(kb_unit, static_cast<double>(rem * cg));
         }
     }
-    if (split > 1) cost += 3000.0 + epi;     // partials round trip and the last arriver's reduction
+    if (split > 1) {
+        // every split parks a fp32 partial; with all split units resident the splits reduce a share
+        // each (parallel), else the last to arrive reads all of them
+        const double part = static_cast<double>(kTcTileN) * bm * 4.0 / 27.0;
+        if (units <= workers) cost += 1500.0 + part + (part * split + epi) / split;
+        else cost += 3000.0 + part + part * split + epi;
+    }
     return cost;
 }
 
@@ -1231,6 +1239,8 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
         e.tiles_n = static_cast<int32_t>((p.n + s.macro_tile1 - 1) / s.macro_tile1);
         e.alpha = p.alpha * scale_of(p.scale_a) * scale_of(p.scale_b);
         e.beta = p.beta;
+        e.tma_store = (p.m > 0 && p.n > 0 &&
+                       tc_encode_output(&e.tmD, p.dtype_d, D[i], p.m, p.n, p.ldd, 1, p.stride_d)) ? 1 : 0;
         prefix[i + 1] = prefix[i] + static_cast<int64_t>(e.tiles_m) * e.tiles_n;
         flops += 2.0 * static_cast<double>(p.m) * p.n * p.k;
     }

@@ -60,7 +60,8 @@ struct TcGroupEntry {   // aligned like CUtensorMap
     int32_t M, N, K;
     int32_t tiles_m, tiles_n;
     float alpha, beta;
-    int32_t pad_;
+    int32_t tma_store;   // tmD describes D: whole tiles leave through TMA stores
+    CUtensorMap tmD;     // problem D, boxes of 128 bytes x 32 rows
 };
 
 struct TcLaunch {
@@ -96,6 +97,9 @@ struct TcLaunch {
 
 // Dynamic shared memory of one CTA staging bm_cta m-rows per stage (bm / 2 for a CTA pair).
 size_t tc_smem_bytes(int bm_cta, int stages);
+// Tensor map of an output for TMA stores (false when TMA cannot address it).
+bool tc_encode_output(CUtensorMap* tm, int out_dtype, void* D, int64_t M, int64_t N, int64_t ldd, int64_t batch,
+                      int64_t stride_d);
 // Persistent workers (CTAs, or co-resident clusters of `cl` CTAs) a tensor-core launch gets.
 int tc_workers(int in_dtype, int out_dtype, int cl, int bm, int stages, int sm_count);
 int tc_tmem_cols(int bm);
