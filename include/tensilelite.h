@@ -129,7 +129,10 @@ typedef struct tl_gemm_solution {
 /* ---- handles and errors --------------------------------------------------------------------- */
 
 /* Create a handle on the current CUDA device (replaces RuntimeHip::GetInstance + SellectDevice,
- * ff_gpu_src/ff_hip_runtime.cpp:8-51; unlike the reference it is not a process singleton). */
+ * ff_gpu_src/ff_hip_runtime.cpp:8-51; unlike the reference it is not a process singleton).  When the
+ * environment variable TL_SOLUTIONS names a file written by tl_tune, its solutions for this device
+ * are loaded (the tuned-solution database that replaces the reference's Tensile LibraryLogic yaml,
+ * test/work/tensile tune). */
 TL_API tl_status tl_init(tl_handle** handle);
 TL_API tl_status tl_destroy(tl_handle* handle);
 /* Message of the last failing call on this host thread ("" if none). */
@@ -170,6 +173,36 @@ TL_API tl_status tl_gemm(tl_handle* handle, const tl_gemm_problem* problem,
 TL_API tl_status tl_tune(tl_handle* handle, const tl_gemm_problem* problem, void* D, const void* C,
                          const void* A, const void* B, int max_candidates, int reps,
                          const char* cache_path, tl_gemm_solution* best, float* best_ms);
+/* ---- fused epilogue ------------------------------------------------------------------------------ */
+
+/* Beyond alpha/beta: the reference fuses the beta*C update into its kernel's store
+ * (src/gemmMfmaKernelWriter.h:1822-1906); tl_gemm_ex fuses a per-row bias, an activation and an
+ * amax reduction the same way:  D = act(alpha*op(A)*op(B) + beta*C + bias[i])  for every element
+ * (i, j) of the m x n output (bias broadcast along n: for a row-major Y = X*W viewed as
+ * column-major, one value per output feature).  When amax is set, max |D| over the computed values
+ * (before rounding to the output type) is atomically maxed into *amax (device float; initialise
+ * it, e.g. to 0, before the call) -- the scale input of a following FP8 quantisation.  Tensor-core
+ * kernels only (TL_ERR_UNSUPPORTED for the CUDA-core kernel). */
+typedef enum tl_activation {
+    TL_ACT_NONE = 0,
+    TL_ACT_RELU = 1,
+    TL_ACT_GELU = 2,   /* tanh approximation: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))) */
+    TL_ACT_SILU = 3    /* x / (1 + exp(-x)) */
+} tl_activation;
+
+typedef struct tl_epilogue {
+    const void* bias;     /* NULL, or m device values of bias_dtype */
+    int32_t bias_dtype;   /* TL_DTYPE_FP32, FP16 or BF16 */
+    int32_t activation;   /* tl_activation */
+    float* amax;          /* NULL, or a device float */
+    int32_t reserved[4];
+} tl_epilogue;
+
+/* tl_gemm with a fused epilogue (epilogue == NULL: tl_gemm). */
+TL_API tl_status tl_gemm_ex(tl_handle* handle, const tl_gemm_problem* problem, const tl_epilogue* epilogue,
+                            const tl_gemm_solution* solution, void* D, const void* C, const void* A, const void* B,
+                            void* stream);
+
 /* ---- Tensile replacement-kernel entry ----------------------------------------------------------- */
 
 /* The argument buffer of the reference's Tensile-layout kernel (`-t 1`, src/gemmMfma.cpp:70-103;

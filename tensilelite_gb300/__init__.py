@@ -93,6 +93,15 @@ class Problem(ctypes.Structure):
         return 2.0 * self.m * self.n * self.k * self.batch
 
 
+ACTIVATIONS = {"none": 0, "relu": 1, "gelu": 2, "silu": 3}
+
+
+class Epilogue(ctypes.Structure):
+    """tl_epilogue: D = act(alpha*op(A)*op(B) + beta*C + bias[row]); max |D| into *amax."""
+    _fields_ = [("bias", ctypes.c_void_p), ("bias_dtype", ctypes.c_int32), ("activation", ctypes.c_int32),
+                ("amax", ctypes.c_void_p), ("reserved", ctypes.c_int32 * 4)]
+
+
 class Solution(ctypes.Structure):
     """tl_gemm_solution: macro tile MT0 x MT1, depth_u, stages (lds_buffer_num), wave tile, split_k."""
     _fields_ = [("kernel", ctypes.c_int32), ("macro_tile0", ctypes.c_int32), ("macro_tile1", ctypes.c_int32),
@@ -155,6 +164,7 @@ def lib():
         "tl_timer_elapsed_ms": [_vp, ctypes.POINTER(f32)], "tl_timer_destroy": [_vp],
         "tl_launch_count": [_vp, ctypes.POINTER(i64)], "tl_device_status": [_vp, _vp],
         "tl_set_kernel_timing": [_vp, i32],
+        "tl_gemm_ex": [_vp, P, ctypes.POINTER(Epilogue), S, _vp, _vp, _vp, _vp, _vp],
         "tl_tensile_launch": [_vp, ctypes.c_char_p, _vp, ctypes.c_size_t, _vp],
         "tl_kernel_timing": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(i64), i32],
         "tl_set_wait_timeout": [_vp, ctypes.c_uint32],
@@ -293,6 +303,20 @@ class Handle:
         n = ctypes.c_int64()
         check(lib().tl_launch_count(self._h, ctypes.byref(n)))
         return n.value
+
+    def gemm_ex(self, p: Problem, D, C, A, B, bias=None, bias_dtype=None, activation="none", amax=None,
+                solution: Optional[Solution] = None, stream=None):
+        """tl_gemm_ex: tl_gemm with a fused bias / activation / amax epilogue."""
+        e = Epilogue()
+        e.bias = _ptr(bias)
+        if bias is not None and bias_dtype is None:
+            bias_dtype = torch_dtype_code(bias.dtype)
+        e.bias_dtype = (DTYPE_NAMES[bias_dtype] if isinstance(bias_dtype, str) else bias_dtype) or FP32
+        e.activation = ACTIVATIONS[activation] if isinstance(activation, str) else int(activation)
+        e.amax = _ptr(amax)
+        check(lib().tl_gemm_ex(self._h, ctypes.byref(p), ctypes.byref(e),
+                               ctypes.byref(solution) if solution is not None else None,
+                               _ptr(D), _ptr(C), _ptr(A), _ptr(B), _stream_ptr(stream)))
 
     def tensile_launch(self, kernel_name: str, kernarg: bytes, stream=None):
         """tl_tensile_launch: the GEMM a Tensile-layout (Cijk_Alik_Bljk) argument buffer describes."""
@@ -498,6 +522,21 @@ def _make_autograd():
 
 
 _TLMatmul = None
+
+
+def linear(X, W, bias=None, activation="none", amax=None):
+    """Inference-only fused Y = act(X @ W + bias) on the tensor-core kernel (row-major X (M, K),
+    W (K, N), bias (N,)); `amax`, a one-element float32 CUDA tensor, receives max |Y| (atomically
+    maxed into it).  No autograd."""
+    import torch
+    Xs, Ws = X.contiguous(), W.contiguous()
+    M, K = Xs.shape
+    N = Ws.shape[1]
+    Y = torch.empty((M, N), dtype=X.dtype, device=X.device)
+    # Y^T = W^T X^T column-major: m = N (bias index), n = M
+    p = Problem.make(N, M, K, dtype=torch_dtype_code(X.dtype), lda=N, ldb=K, ldd=N)
+    default_handle().gemm_ex(p, Y, None, Ws, Xs, bias=bias, activation=activation, amax=amax)
+    return Y
 
 
 def matmul(X, W):

@@ -19,6 +19,31 @@ LIB = os.path.join(HERE, "libtensilelite_gb300.so")
 CLI = os.path.join(HERE, "tensilelite")
 
 SOURCES = ["gemm_tc.cu", "gemm_simt.cu", "aux_kernels.cu", "tl_api.cpp", "noalloc.cu"]
+# The tcgen05 kernel template is instantiated in generated units, one per operand kind (0 fp16/bf16,
+# 1 fp8), cluster size and epilogue variant (three output types each), so they compile in parallel.
+INSTANCES = [(k, e, cl) for k in (0, 1) for e in ((False, True) if k == 0 else (False,)) for cl in (1, 2, 4)]
+OUT_TYPES = ("float", "__half", "__nv_bfloat16")
+
+
+def _instance_sources():
+    gen = os.path.join(BUILD, "gen")
+    os.makedirs(gen, exist_ok=True)
+    paths = []
+    for k, e, cl in INSTANCES:
+        lines = ['#include "tensilelite_gb300/csrc/gemm_tc_kernel.cuh"', "namespace tl {", "namespace tc {"]
+        for td in OUT_TYPES:
+            lines.append(f"template tl_status launch_kernel<{k}, {td}, {cl}, {'true' if e else 'false'}>("
+                         "const TcKernelParams&, int, size_t, cudaStream_t);")
+            if not e:
+                lines.append(f"template int max_clusters<{k}, {td}, {cl}>(size_t);")
+        lines += ["}  // namespace tc", "}  // namespace tl", ""]
+        text = "\n".join(lines)
+        path = os.path.join(gen, f"tc_k{k}_e{int(e)}_c{cl}.cu")
+        if not os.path.exists(path) or open(path).read() != text:
+            with open(path, "w") as f:
+                f.write(text)
+        paths.append(path)
+    return paths
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I" + ROOT]
 
@@ -51,8 +76,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     nv = nvcc()
     jobs = []
     objs = []
-    for src in SOURCES:
-        path = os.path.join(CSRC, src)
+    for path in [os.path.join(CSRC, src) for src in SOURCES] + _instance_sources():
+        src = os.path.basename(path)
         obj = os.path.join(BUILD, src + ".o")
         objs.append(obj)
         if force or _stale(obj, [path] + headers):

@@ -460,6 +460,8 @@ struct Prepared {
     int64_t a_span = 0, b_span = 0;
     float* ws_partials = nullptr;
     size_t part_bytes = 0;
+    tl_epilogue epi{};
+    bool epi_on = false;
 };
 
 int64_t operand_span(int64_t ld, int64_t cols, int64_t batch, int64_t bstride, int64_t rows)
@@ -685,6 +687,11 @@ tl_status enqueue(tl_handle* h, const Prepared& P, cudaStream_t s)
     L.counters_len = h->counters_len;
     L.tail_split = P.s.tail_split;
     L.sm_count = h->sm_count;
+    L.epi_on = P.epi_on ? 1 : 0;
+    L.epi_bias = P.epi.bias;
+    L.epi_amax = P.epi.amax;
+    L.epi_bias_dtype = P.epi.bias_dtype;
+    L.epi_act = P.epi.activation;
     const bool timed = timing_begin(h, s);
     const tl_status st = tc_gemm_launch(L, s, &h->launches);
     timing_end(h, s, timed, st);
@@ -878,6 +885,11 @@ TL_API tl_status tl_init(tl_handle** handle)
     h->d_norms = reinterpret_cast<double*>(reinterpret_cast<char*>(h->d_err) + 64);
     h->d_amax = reinterpret_cast<float*>(reinterpret_cast<char*>(h->d_err) + 128);
     if ((e = cudaMemset(h->d_err, 0, 256)) != cudaSuccess) { cudaFree(h->d_err); delete h; return cuda_fail(e, "cudaMemset"); }
+    // the tuned-solution database of this device, when TL_SOLUTIONS names one (a missing file is no error)
+    if (const char* path = getenv("TL_SOLUTIONS")) {
+        std::ifstream probe(path);
+        if (probe) tl_load_solutions(h, path, nullptr);
+    }
     *handle = h;
     return TL_SUCCESS;
 }
@@ -1063,6 +1075,36 @@ TL_API tl_status tl_tensile_launch(tl_handle* h, const char* kernel_name, const 
                     (beta != 0.0f && tn_extent(M, N, st[2], batch, st[3]) > size_c))))
         return fail(TL_ERR_INVALID_ARG, "Tensile arguments: strides and sizes exceed a declared buffer size");
     return tl_gemm(h, &p, nullptr, D, C, A, B, stream);
+}
+
+TL_API tl_status tl_gemm_ex(tl_handle* h, const tl_gemm_problem* p, const tl_epilogue* epi,
+                            const tl_gemm_solution* s, void* D, const void* C, const void* A, const void* B, void* stream)
+{
+    if (!h) return fail(TL_ERR_INVALID_ARG, "handle is NULL");
+    if (!epi) return tl_gemm(h, p, s, D, C, A, B, stream);
+    if (epi->activation < TL_ACT_NONE || epi->activation > TL_ACT_SILU)
+        return fail(TL_ERR_INVALID_ARG, "epilogue activation must be NONE, RELU, GELU or SILU");
+    if (epi->bias && epi->bias_dtype != TL_DTYPE_FP32 && epi->bias_dtype != TL_DTYPE_FP16 &&
+        epi->bias_dtype != TL_DTYPE_BF16)
+        return fail(TL_ERR_INVALID_ARG, "epilogue bias must be fp32, fp16 or bf16");
+    if (epi->bias && (reinterpret_cast<uintptr_t>(epi->bias) % dtype_bytes(epi->bias_dtype)))
+        return fail(TL_ERR_INVALID_ARG, "epilogue bias is not aligned to its element size");
+    if (epi->amax && (reinterpret_cast<uintptr_t>(epi->amax) & 3))
+        return fail(TL_ERR_INVALID_ARG, "epilogue amax is not 4-byte aligned");
+    Prepared P;
+    t_capturing = stream_capturing(S(stream));
+    if (t_capturing) h->captured = true;
+    tl_status st = prepare(h, p, s, D, C, A, B, &P);
+    t_capturing = false;
+    if (st != TL_SUCCESS) return st;
+    if (P.kernel == TL_KERNEL_SIMT)
+        return fail(TL_ERR_UNSUPPORTED, "a fused epilogue needs a tensor-core kernel (fp16/bf16/fp8 operands, or "
+                                        "fp32 with BF16X3/BF16X6)");
+    if (P.p.k == 0 || P.p.m == 0 || P.p.n == 0)
+        return fail(TL_ERR_UNSUPPORTED, "a fused epilogue needs m, n, k > 0");
+    P.epi = *epi;
+    P.epi_on = epi->bias != nullptr || epi->activation != TL_ACT_NONE || epi->amax != nullptr;
+    return enqueue(h, P, S(stream));
 }
 
 TL_API tl_status tl_tune(tl_handle* h, const tl_gemm_problem* p, void* D, const void* C, const void* A,

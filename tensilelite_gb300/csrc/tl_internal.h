@@ -93,6 +93,12 @@ struct TcLaunch {
     size_t counters_len;
     int tail_split;          // 0 auto, 1 off, S: k splits of the last partial wave's tiles
     int sm_count;
+    // fused epilogue: D = act(alpha*acc + beta*C + bias[m]); max |D| into *epi_amax
+    const void* epi_bias;
+    float* epi_amax;
+    int epi_bias_dtype;
+    int epi_act;
+    int epi_on;
 };
 
 // Dynamic shared memory of one CTA staging bm_cta m-rows per stage (bm / 2 for a CTA pair).

@@ -718,3 +718,84 @@ def test_cli_runs_and_verifies(args):
     assert "Performance =" in out.stdout
     if "-t" not in args:
         assert "Verify Success" in out.stdout, out.stdout
+
+
+# ---------------------------------------------------------------------------- fused epilogue
+def _epi_ref(o, bias, act):
+    o = o.astype(np.float32)
+    if bias is not None:
+        o = (o + bias.astype(np.float32)[:, None]).astype(np.float32)
+    if act == "relu":
+        o = np.maximum(o, 0)
+    elif act == "gelu":
+        x = o.astype(np.float64)
+        o = (0.5 * x * (1 + np.tanh(0.7978845608028654 * (x + 0.044715 * x ** 3)))).astype(np.float32)
+    elif act == "silu":
+        x = o.astype(np.float64)
+        o = (x / (1 + np.exp(-x))).astype(np.float32)
+    return o
+
+
+@pytest.mark.parametrize("dt,lay,act,cg,bm,split", [
+    ("bf16", "NN", "gelu", 2, 256, 1), ("bf16", "TN", "relu", 4, 256, 1), ("fp16", "NT", "silu", 1, 128, 1),
+    ("bf16", "NN", "none", 1, 128, 3), ("fp16", "TN", "gelu", 2, 128, 2)])
+def test_fused_epilogue(h, dt, lay, act, cg, bm, split):
+    """tl_gemm_ex: act(alpha*AB + beta*C + bias[m]) and max |D| against the same kernel's fp32-output
+    result with the epilogue applied on the host (one output ulp), ragged sizes, whole tiles (TMA
+    stores) and split-k reductions."""
+    import torch
+    m, n, k = 1000, 600, 320
+    case = gg.make_case(dt, lay, 321 + cg + bm + split, m, n, k, alpha=0.75, beta=0.5, ld_align=8)
+    A, B = gu.to_dev(case["A_bits"], dt), gu.to_dev(case["B_bits"], dt)
+    C = gu.to_dev(case["C_bits"], dt)
+    tdt = {"bf16": torch.bfloat16, "fp16": torch.float16}[dt]
+    g = np.random.default_rng(5)
+    bias = g.standard_normal(m).astype(np.float32)
+    dbias = torch.from_numpy(bias).cuda()
+    sol = tl.Solution(kernel=tl.KERNEL_TCGEN05, macro_tile0=bm, macro_tile1=128 * cg, depth_u=0, stages=4,
+                      split_k=split)
+    kw = dict(trans_a=lay[0] == "T", trans_b=lay[1] == "T", alpha=0.75, beta=0.5, lda=case["lda"], ldb=case["ldb"],
+              kernel="tcgen05")
+    # the pre-epilogue values: same kernel and solution with fp32 output (C widened exactly)
+    p32 = tl.Problem.make(m, n, k, dtype=dt, out_dtype="fp32", **kw)
+    C32 = torch.from_numpy(case["C"].astype(np.float32)).cuda()
+    D32 = torch.empty(m * n, dtype=torch.float32, device="cuda")
+    h.gemm(p32, D32, C32, A, B, solution=sol)
+    p = tl.Problem.make(m, n, k, dtype=dt, **kw)
+    D = torch.empty(m * n, dtype=tdt, device="cuda")
+    amax = torch.zeros(1, dtype=torch.float32, device="cuda")
+    h.gemm_ex(p, D, C, A, B, bias=dbias, activation=act, amax=amax, solution=sol)
+    torch.cuda.synchronize()
+    h.device_status()
+    ref = _epi_ref(D32.cpu().numpy().reshape(n, m).T, bias, act)
+    got = D.float().cpu().numpy().reshape(n, m).T
+    # one output ulp, with an absolute floor for the activations' flat tails (gelu / silu of large
+    # negative inputs cancel to ~1e-10 in float64 but to 0 on the device)
+    mant = {"bf16": 7, "fp16": 10}[dt]
+    mag = np.maximum(np.abs(ref).astype(np.float64), 2.0 ** -126)
+    ulp = 2.0 ** (np.floor(np.log2(mag)) - mant)
+    bad = np.abs(got.astype(np.float64) - ref) > ulp + 1e-6 * np.abs(ref).max()
+    assert int(bad.sum()) == 0, (got[bad][:5], ref[bad][:5])
+    assert abs(amax.item() - np.abs(ref).max()) <= 1e-5 * np.abs(ref).max()
+
+
+def test_fused_epilogue_errors_and_linear(h):
+    import torch
+    p = tl.Problem.make(64, 64, 64, dtype="fp32")
+    X = torch.randn(64 * 64, device="cuda")
+    with pytest.raises(tl.TLError) as e:
+        h.gemm_ex(p, torch.empty_like(X), None, X, X, activation="relu")      # CUDA-core kernel
+    assert e.value.status == tl.ERR_UNSUPPORTED
+    pb = tl.Problem.make(64, 64, 64, dtype="bf16")
+    Xb = X.to(torch.bfloat16)
+    with pytest.raises(tl.TLError) as e:
+        h.gemm_ex(pb, torch.empty_like(Xb), None, Xb, Xb, activation=7)
+    assert e.value.status == tl.ERR_INVALID_ARG
+    # row-major fused linear layer against torch in fp32
+    g = torch.Generator(device="cuda").manual_seed(9)
+    Xr = torch.randn(512, 384, device="cuda", generator=g).to(torch.bfloat16)
+    Wr = (torch.randn(384, 768, device="cuda", generator=g) * 0.05).to(torch.bfloat16)
+    br = torch.randn(768, device="cuda", generator=g).to(torch.bfloat16)
+    Y = tl.linear(Xr, Wr, br, "gelu")
+    ref = torch.nn.functional.gelu(Xr.float() @ Wr.float() + br.float(), approximate="tanh")
+    assert float((Y.float() - ref).abs().max() / ref.abs().max()) < 1e-2
