@@ -255,24 +255,29 @@ def barrier(world):
         dist.barrier()
 
 
-def max_over_ranks(x, world):
-    if world == 1:
-        return x
+def _reduce(x, op):
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def max_over_ranks(x, world):
+    """The slowest rank's time (every rank ran its replica of the workload)."""
+    if world == 1:
+        return x
+    import torch.distributed as dist
+    return _reduce(x, dist.ReduceOp.MAX)
 
 
 def sum_over_ranks(x, world):
+    """The work all ranks did together."""
     if world == 1:
         return x
-    import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return _reduce(x, dist.ReduceOp.SUM)
 
 
 def run_gpu(args, w, name):
