@@ -585,7 +585,10 @@ def run_grouped(args, w, name):
         D.append(torch.empty(m * n, device="cuda", dtype=torch.bfloat16))
         probs.append(tl.Problem.make(m, n, k, dtype="bf16", alpha=w["alpha"], beta=w["beta"], kernel="tcgen05"))
     flops = sum(2.0 * m * n * k for m, n, k in sizes)
-    sol, tuned_ms = h.tune_grouped(probs, D, None, A, B, reps=3)
+    if args.no_tune_grouped:
+        sol, tuned_ms = None, 0.0            # the plan's heuristic tile (profiling runs)
+    else:
+        sol, tuned_ms = h.tune_grouped(probs, D, None, A, B, reps=3)
     plan = h.grouped_plan(probs, D, None, A, B, solution=sol)
     stream = torch.cuda.Stream()
     graph = plan.capture(stream)
@@ -872,6 +875,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-check", dest="check", action="store_false")
+    ap.add_argument("--no-tune-grouped", action="store_true",
+                    help="grouped256: use the plan's heuristic tile instead of tl_tune_grouped")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
