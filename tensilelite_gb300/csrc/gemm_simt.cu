@@ -3,7 +3,8 @@
 // The plain-FP32 counterpart of TensileLite's sgemm path (the fp32 MFMA kernel,
 // src/gemmMfmaKernelWriter.h:38-40) and the generic fallback for operands the TMA path cannot
 // describe (leading dimensions that are not 16-byte multiples).  128x128 output tile per 256-thread
-// CTA, 8x8 outputs per thread in two 4-wide strips per dimension, k staged 8 at a time through a
+// CTA, 8x8 outputs per thread in two 4-wide strips per dimension (or, when 128x128 tiles would leave
+// most SMs idle, 64x64 tiles with 4x4 outputs per thread), k staged 8 at a time through a
 // double-buffered shared-memory ring with the next slab prefetched into registers.  op(A)/op(B) of
 // either storage order are read with the thread mapping that keeps the contiguous dimension
 // coalesced; edge tiles are zero-filled on load and masked on store.
@@ -16,7 +17,7 @@
 namespace tl {
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 8, THREADS = 256;
+constexpr int BK = 8, THREADS = 256;
 
 template <typename T> __device__ __forceinline__ float to_f(T v);
 template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
@@ -46,9 +47,13 @@ struct SimtParams {
     int out_trunc;
 };
 
-template <typename TA, typename TD>
+// TM outputs per thread and dimension: 8 (128 x 128 tile) or 4 (64 x 64 tile), in TM/4 strips of 4
+template <typename TA, typename TD, int TM>
 __global__ void __launch_bounds__(THREADS, 2) simt_gemm_kernel(const SimtParams p)
 {
+    constexpr int BM = 16 * TM, BN = 16 * TM;   // 16 x 16 threads
+    constexpr int LOADS = BM * BK / THREADS;    // elements of A (and of B) each thread stages per slab
+    constexpr int STRIPS = TM / 4;
     __shared__ __align__(16) float As[2][BK][BM];
     __shared__ __align__(16) float Bs[2][BK][BN];
 
@@ -61,20 +66,20 @@ __global__ void __launch_bounds__(THREADS, 2) simt_gemm_kernel(const SimtParams 
     const TA* A = static_cast<const TA*>(p.A) + static_cast<int64_t>(b) * p.sa;
     const TA* B = static_cast<const TA*>(p.B) + static_cast<int64_t>(b) * p.sb;
 
-    // per-thread load coordinates: 4 elements of A and 4 of B per k-slab
-    int a_m[4], a_k[4], b_n[4], b_k[4];
+    // per-thread load coordinates: LOADS elements of A and of B per k-slab
+    int a_m[LOADS], a_k[LOADS], b_n[LOADS], b_k[LOADS];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < LOADS; ++i) {
         const int idx = tid + i * THREADS;
         if (!p.trans_a) { a_m[i] = idx % BM; a_k[i] = idx / BM; }   // A[m + k*lda]: m contiguous
         else { a_m[i] = idx / BK; a_k[i] = idx % BK; }              // A[k + m*lda]: k contiguous
         if (p.trans_b) { b_n[i] = idx % BN; b_k[i] = idx / BN; }    // B[n + k*ldb]: n contiguous
         else { b_n[i] = idx / BK; b_k[i] = idx % BK; }              // B[k + n*ldb]: k contiguous
     }
-    float ra[4], rb[4];
+    float ra[LOADS], rb[LOADS];
     auto load_slab = [&](int k0) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < LOADS; ++i) {
             const int m = m_blk + a_m[i], k = k0 + a_k[i];
             float v = 0.f;
             if (m < p.M && k < p.K)
@@ -89,17 +94,17 @@ __global__ void __launch_bounds__(THREADS, 2) simt_gemm_kernel(const SimtParams 
     };
     auto store_slab = [&](int buf) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < LOADS; ++i) {
             As[buf][a_k[i]][a_m[i]] = ra[i];
             Bs[buf][b_k[i]][b_n[i]] = rb[i];
         }
     };
 
-    float acc[8][8];
+    float acc[TM][TM];
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
+    for (int i = 0; i < TM; ++i)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+        for (int j = 0; j < TM; ++j) acc[i][j] = 0.f;
 
     const int nslab = (p.K + BK - 1) / BK;
     if (nslab > 0) {
@@ -112,16 +117,18 @@ __global__ void __launch_bounds__(THREADS, 2) simt_gemm_kernel(const SimtParams 
         if (s + 1 < nslab) load_slab((s + 1) * BK);
 #pragma unroll
         for (int k = 0; k < BK; ++k) {
-            const float4 a0 = *reinterpret_cast<const float4*>(&As[buf][k][tx * 4]);
-            const float4 a1 = *reinterpret_cast<const float4*>(&As[buf][k][64 + tx * 4]);
-            const float4 b0 = *reinterpret_cast<const float4*>(&Bs[buf][k][ty * 4]);
-            const float4 b1 = *reinterpret_cast<const float4*>(&Bs[buf][k][64 + ty * 4]);
-            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-            const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+            float a[TM], bb[TM];
 #pragma unroll
-            for (int i = 0; i < 8; ++i)
+            for (int st = 0; st < STRIPS; ++st) {
+                const float4 av = *reinterpret_cast<const float4*>(&As[buf][k][st * 64 + tx * 4]);
+                const float4 bv = *reinterpret_cast<const float4*>(&Bs[buf][k][st * 64 + ty * 4]);
+                a[4 * st] = av.x; a[4 * st + 1] = av.y; a[4 * st + 2] = av.z; a[4 * st + 3] = av.w;
+                bb[4 * st] = bv.x; bb[4 * st + 1] = bv.y; bb[4 * st + 2] = bv.z; bb[4 * st + 3] = bv.w;
+            }
 #pragma unroll
-                for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], bb[j], acc[i][j]);
+            for (int i = 0; i < TM; ++i)
+#pragma unroll
+                for (int j = 0; j < TM; ++j) acc[i][j] = fmaf(a[i], bb[j], acc[i][j]);
         }
         if (s + 1 < nslab) store_slab(buf ^ 1);
         __syncthreads();
@@ -132,12 +139,12 @@ __global__ void __launch_bounds__(THREADS, 2) simt_gemm_kernel(const SimtParams 
     const TD* C = p.C ? static_cast<const TD*>(p.C) + static_cast<int64_t>(b) * p.sc : nullptr;
     const bool use_c = (p.beta != 0.f) && (C != nullptr);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        const int n = n_blk + (j < 4 ? ty * 4 + j : 64 + ty * 4 + (j - 4));
+    for (int j = 0; j < TM; ++j) {
+        const int n = n_blk + (j / 4) * 64 + ty * 4 + (j % 4);
         if (n >= p.N) continue;
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int m = m_blk + (i < 4 ? tx * 4 + i : 64 + tx * 4 + (i - 4));
+        for (int i = 0; i < TM; ++i) {
+            const int m = m_blk + (i / 4) * 64 + tx * 4 + (i % 4);
             if (m >= p.M) continue;
             float v = p.alpha * acc[i][j];
             if (use_c) v = fmaf(p.alpha, acc[i][j], p.beta * load_out<TD>(C + m + static_cast<int64_t>(n) * p.ldc));
@@ -157,9 +164,23 @@ tl_status launch(const SimtLaunch& L, cudaStream_t s)
     p.trans_a = L.trans_a; p.trans_b = L.trans_b;
     p.alpha = L.alpha; p.beta = L.beta;
     p.out_trunc = L.out_trunc;
-    dim3 grid(static_cast<unsigned>((L.M + BM - 1) / BM), static_cast<unsigned>((L.N + BN - 1) / BN),
-              static_cast<unsigned>(L.batch));
-    simt_gemm_kernel<TA, TD><<<grid, THREADS, 0, s>>>(p);
+    // 128 x 128 tiles, or 64 x 64 when the larger tiles would occupy fewer than half of the SMs
+    static const int sms = [] {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        return n > 0 ? n : 1;
+    }();
+    const int64_t big_tiles = ((L.M + 127) / 128) * ((L.N + 127) / 128) * L.batch;
+    if (2 * big_tiles < sms) {
+        dim3 grid(static_cast<unsigned>((L.M + 63) / 64), static_cast<unsigned>((L.N + 63) / 64),
+                  static_cast<unsigned>(L.batch));
+        simt_gemm_kernel<TA, TD, 4><<<grid, THREADS, 0, s>>>(p);
+    } else {
+        dim3 grid(static_cast<unsigned>((L.M + 127) / 128), static_cast<unsigned>((L.N + 127) / 128),
+                  static_cast<unsigned>(L.batch));
+        simt_gemm_kernel<TA, TD, 8><<<grid, THREADS, 0, s>>>(p);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "simt_gemm_kernel launch");
     return TL_SUCCESS;
@@ -182,7 +203,7 @@ tl_status simt_gemm_launch(const SimtLaunch& L, cudaStream_t s, int64_t* launche
 {
     if (L.M > 0x7fffffff || L.N > 0x7fffffff || L.K > 0x7fffffff || L.batch > 65535)
         return fail(TL_ERR_UNSUPPORTED, "SIMT kernel: dimension too large");
-    if ((L.N + BN - 1) / BN > 65535) return fail(TL_ERR_UNSUPPORTED, "SIMT kernel: n too large");
+    if ((L.N + 63) / 64 > 65535) return fail(TL_ERR_UNSUPPORTED, "SIMT kernel: n too large");
     tl_status st;
     switch (L.a_dtype) {
     case TL_DTYPE_FP32: st = launch_out<float>(L, s); break;
