@@ -173,6 +173,16 @@ bool cluster4_enabled()
     return on;
 }
 
+// Grouped plans order their problems by decreasing k unless TL_GROUP_ORDER=0 in the environment.
+bool group_order_by_k()
+{
+    static const bool on = [] {
+        const char* e = getenv("TL_GROUP_ORDER");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 int max_stages(int bm_cta, size_t smem_optin)
 {
     int s = kTcMaxStages;
@@ -1292,7 +1302,15 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
     const int64_t total_units = prefix[count];
     if (total_units > INT32_MAX) return fail(TL_ERR_UNSUPPORTED, "grouped plan has too many tiles");
     std::vector<int4> units(static_cast<size_t>(total_units));
-    for (int i = 0, w = 0; i < count; ++i) {
+    // problems in order of decreasing k: the tiles running side by side then take about as long,
+    // so the workers stay in step (tiles sharing operand rows read them while they are in L2) and
+    // the launch ends with its shortest tiles
+    std::vector<int> order(count);
+    for (int i = 0; i < count; ++i) order[i] = i;
+    if (group_order_by_k())
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return host[a].K > host[b].K; });
+    for (int oi = 0, w = 0; oi < count; ++oi) {
+        const int i = order[oi];
         const TcGroupEntry& e = host[i];
         const int nkb = static_cast<int>((e.K + kb_elems - 1) / kb_elems);
         for (int in = 0; in < e.tiles_n; ++in)
