@@ -100,16 +100,6 @@ EncodeTiledFn get_encode_fn()
     return fn;
 }
 
-// Two ring slots per barrier handshake: on unless TL_KPS2=0 in the environment.
-bool kps2_enabled()
-{
-    static const bool on = [] {
-        const char* e = getenv("TL_KPS2");
-        return !(e && e[0] == '0');
-    }();
-    return on;
-}
-
 // Parallel split-k reduction: on unless TL_PAR_REDUCE=0 in the environment.
 bool par_reduce_enabled()
 {
@@ -438,8 +428,6 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
         kp.par_reduce = (kp.split_units > 0 && kp.bal_kb == 0 && kp.split_units <= workers && par_reduce_enabled()) ? 1 : 0;
     }
     // whole tiles leave through TMA stores (not with promotion, which drains chains into registers)
-    // two ring slots per barrier handshake where every slot holds a plain product
-    kp.kps = (kp.nterms == 1 && L.promote_k == 0 && L.stages % 2 == 0 && kps2_enabled()) ? 2 : 1;
     kp.tma_store = (L.promote_k == 0 && tma_store_enabled() &&
                     tc_encode_output(&kp.tmD, L.out_dtype, L.D, L.M, L.N, L.ldd, L.batch, L.stride_d))
                        ? 1
@@ -463,7 +451,6 @@ tl_status tc_grouped_launch(const TcGroupLaunch& G, cudaStream_t stream, int64_t
     kp.stages = G.stages;
     kp.split_k = 1;
     kp.nterms = 1;
-    kp.kps = (G.stages % 2 == 0 && kps2_enabled()) ? 2 : 1;
     kp.total_work = G.total_tiles;
     kp.split_units = 0;
     kp.split_tiles = 0;

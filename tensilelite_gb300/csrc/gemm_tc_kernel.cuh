@@ -22,8 +22,6 @@ struct TcKernelParams {
     CUtensorMap tmN[3], tmM[3];   // split-precision pieces 0..2 (piece 0 = the operand itself)
     CUtensorMap tmD;              // the output, boxes of 128 bytes x 32 rows (tma_store)
     int tma_store;                // whole tiles leave through shared memory and TMA stores
-    int kps;                      // ring slots per full/empty barrier handshake (1, or 2 without
-                                  // promotion and split products); a group never spans two tiles
     // fused epilogue (kernels instantiated with EPI): D = act(alpha*acc + beta*C + bias[m]), and
     // max |D| into *epi_amax
     const void* epi_bias;
@@ -787,7 +785,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             constexpr int W = kTcRowBytes / (KIND == 0 ? 2 : 1);   // elements per 128-byte row
             const int n_mn = p.n_mn_major, m_mn = p.m_mn_major;
             const int nstages = p.stages;
-            const int kps = p.kps;
             bool ok = true;
             int4 u_next = load_unit(p, unit0);
             for (int64_t w = unit0; w < p.total_work && ok; w += units) {
@@ -800,11 +797,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 const int total = (j.kb1 - j.kb0) * nvirt;
                 int kb = j.kb0, v = 0;
                 for (int i = 0; i < total; ++i) {
-                    // ring slot `stage`; its barriers are those of its group of kps slots
-                    const int q = static_cast<int>(stage) % kps;
-                    const uint32_t g = stage / static_cast<uint32_t>(kps);
-                    const uint32_t nq = static_cast<uint32_t>(min(kps - q, total - i));   // at q == 0: slots used
-                    if (q == 0 && !__all_sync(0xffffffffu, ptx::mbar_wait(&empty[g], phase ^ 1u, tlim))) {
+                    if (!__all_sync(0xffffffffu, ptx::mbar_wait(&empty[stage], phase ^ 1u, tlim))) {
                         if (lane == 0) record_error(p, abort_flag, 1);
                         ok = false;
                         break;
@@ -820,8 +813,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                             // the leader arms its full barrier with both CTAs' bytes; the peer's loads
                             // only complete transactions on it (they cannot run a phase ahead: the
                             // peer refills a slot only after the leader's MMAs released it)
-                            const uint32_t fb = ptx::mapa_shared(ptx::smem_u32(&full[g]), pair_base);
-                            if (leader && q == 0) ptx::mbar_arrive_expect_tx(&full[g], 2u * nq * stage_bytes);
+                            const uint32_t fb = ptx::mapa_shared(ptx::smem_u32(&full[stage]), pair_base);
+                            if (leader) ptx::mbar_arrive_expect_tx(&full[stage], 2u * stage_bytes);
                             if (!n_mn) {
                                 ptx::tma_load_3d_pair(sN, mapN, fb, k0, n0, j.b);
                             } else {
@@ -849,28 +842,26 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                                         ptx::tma_load_3d_pair(sM + c * W * kTcRowBytes, mapM, fb, m0 + c * W, k0, j.b);
                             }
                         } else {
-                            if (q == 0) ptx::mbar_arrive_expect_tx(&full[g], nq * stage_bytes);
+                            ptx::mbar_arrive_expect_tx(&full[stage], stage_bytes);
                             if (!n_mn) {
-                                ptx::tma_load_3d(sN, mapN, &full[g], k0, n0, j.b);
+                                ptx::tma_load_3d(sN, mapN, &full[stage], k0, n0, j.b);
                             } else {
 #pragma unroll
                                 for (int c = 0; c < kTcTileN / W; ++c)
-                                    ptx::tma_load_3d(sN + c * W * kTcRowBytes, mapN, &full[g], n0 + c * W, k0, j.b);
+                                    ptx::tma_load_3d(sN + c * W * kTcRowBytes, mapN, &full[stage], n0 + c * W, k0, j.b);
                             }
                             if (!m_mn) {
-                                ptx::tma_load_3d(sM, mapM, &full[g], k0, m0, j.b);
+                                ptx::tma_load_3d(sM, mapM, &full[stage], k0, m0, j.b);
                             } else {
 #pragma unroll
                                 for (int c = 0; c < 4; ++c)      // bmc / W <= 4 chunks
                                     if (c * W < static_cast<int>(bmc))
-                                        ptx::tma_load_3d(sM + c * W * kTcRowBytes, mapM, &full[g], m0 + c * W, k0, j.b);
+                                        ptx::tma_load_3d(sM + c * W * kTcRowBytes, mapM, &full[stage], m0 + c * W, k0, j.b);
                             }
                         }
                     }
                     __syncwarp();
-                    // the last slot of a group, or of the tile: move to the next group's first slot
-                    stage += (q == kps - 1 || i + 1 == total) ? static_cast<uint32_t>(kps - q) : 1u;
-                    if (stage == static_cast<uint32_t>(nstages)) {
+                    if (++stage == static_cast<uint32_t>(nstages)) {
                         stage = 0;
                         phase ^= 1u;
                     }
@@ -897,7 +888,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             const uint32_t n_kstep = p.n_kstep, m_kstep = p.m_kstep, n_lbo = p.n_lbo, m_lbo = p.m_lbo;
             const uint32_t bmu = static_cast<uint32_t>(p.bm);
             const int nstages = p.stages;
-            const int kps = p.kps;
             bool ok = true;
             int4 u_next = load_unit(p, unit0);
             for (int64_t w = unit0; w < p.total_work && ok; w += units) {
@@ -926,17 +916,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 const int total = nkb * nvirt;
                 int v = 0, kb_in_chain = 0;
                 for (int i = 0; i < total; ++i) {
-                    const int q = static_cast<int>(stage) % kps;           // slot within its group
-                    const uint32_t g = stage / static_cast<uint32_t>(kps);
-                    const bool group_end = (q == kps - 1) || (i + 1 == total);
-                    if (q == 0) {
-                        if (!__all_sync(0xffffffffu, ptx::mbar_wait(&full[g], phase, tlim))) {
-                            if (lane == 0) record_error(p, abort_flag, 4);
-                            ok = false;
-                            break;
-                        }
-                        ptx::tc_fence_after();
+                    if (!__all_sync(0xffffffffu, ptx::mbar_wait(&full[stage], phase, tlim))) {
+                        if (lane == 0) record_error(p, abort_flag, 4);
+                        ok = false;
+                        break;
                     }
+                    ptx::tc_fence_after();
                     const bool is_main = !sep_small || v == nvirt - 1;
                     const uint32_t d_tmem = tmem_base + (is_main ? mbuf * bmu : (2u + sbuf) * bmu);
                     const bool started = is_main ? main_started : small_started;
@@ -956,18 +941,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                                 else ptx::mma_f8(d_tmem, adesc, bdesc, idesc, accumulate);
                             }
                         }
-                        // the group's slots are released when its last MMAs complete (MC == 2: in
-                        // every CTA of the cluster)
-                        if (group_end) {
-                            if constexpr (CG == 2) ptx::mma_commit_pair(&empty[g], MC == 2 ? 0xF : 0x3);
-                            else ptx::mma_commit(&empty[g]);
-                        }
+                        // both pairs' ring slots are released (MC == 2: every CTA of the cluster)
+                        if constexpr (CG == 2) ptx::mma_commit_pair(&empty[stage], MC == 2 ? 0xF : 0x3);
+                        else ptx::mma_commit(&empty[stage]);
                     }
                     __syncwarp();
                     main_started = main_started || is_main;
                     small_started = small_started || !is_main;
-                    stage += group_end ? static_cast<uint32_t>(kps - q) : 1u;
-                    if (stage == static_cast<uint32_t>(nstages)) {
+                    if (++stage == static_cast<uint32_t>(nstages)) {
                         stage = 0;
                         phase ^= 1u;
                     }
