@@ -120,6 +120,16 @@ bool tma_store_enabled()
     return on;
 }
 
+// A CTA's last tile is written with direct stores unless TL_LAST_DIRECT=0 in the environment.
+bool last_direct_enabled()
+{
+    static const bool on = [] {
+        const char* e = getenv("TL_LAST_DIRECT");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 // Programmatic dependent launch for the tensor-core kernel: on unless TL_PDL=0 in the environment.
 bool pdl_enabled()
 {
@@ -432,6 +442,7 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
                     tc_encode_output(&kp.tmD, L.out_dtype, L.D, L.M, L.N, L.ldd, L.batch, L.stride_d))
                        ? 1
                        : 0;
+    kp.direct_last = last_direct_enabled() ? 1 : 0;
     kp.ws = L.workspace;
     kp.counters = L.counters;
     kp.err = L.err;
@@ -447,6 +458,7 @@ tl_status tc_grouped_launch(const TcGroupLaunch& G, cudaStream_t stream, int64_t
     memset(&kp, 0, sizeof(kp));
     kp.group = G.d_entries;
     kp.group_units = G.d_units;
+    kp.direct_last = last_direct_enabled() ? 1 : 0;
     kp.bm = G.bm;
     kp.stages = G.stages;
     kp.split_k = 1;

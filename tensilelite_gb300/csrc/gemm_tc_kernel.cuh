@@ -22,6 +22,7 @@ struct TcKernelParams {
     CUtensorMap tmN[3], tmM[3];   // split-precision pieces 0..2 (piece 0 = the operand itself)
     CUtensorMap tmD;              // the output, boxes of 128 bytes x 32 rows (tma_store)
     int tma_store;                // whole tiles leave through shared memory and TMA stores
+    int direct_last;              // a CTA's last tile (beta == 0) leaves through direct stores
     // fused epilogue (kernels instantiated with EPI): D = act(alpha*acc + beta*C + bias[m]), and
     // max |D| into *epi_amax
     const void* epi_bias;
@@ -1117,7 +1118,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             }
             const uint32_t tbase = tmem_base + lane_off + mbuf * static_cast<uint32_t>(p.bm);
             if (ok) ptx::tc_fence_after();
-            if (j.nsplit == 1 && j.tmD != nullptr) {
+            // A staged TMA store costs a round trip per 32 rows (the one 4 KB buffer per warp is
+            // refilled only after the previous store has read it): hidden behind the next tile's
+            // main loop, but exposed on a CTA's last tile, which uses the direct stores instead
+            // when beta == 0 (with a C operand to read, the staged path measured faster).
+            const bool direct = p.direct_last && j.beta == 0.0f && w + units >= p.total_work;
+            if (j.nsplit == 1 && j.tmD != nullptr && !direct) {
                 // each warp stages its 32 rows x 128 bytes of output (128-byte swizzle: 16-byte unit
                 // u of row r sits at u ^ (r & 7)) and writes them with one TMA store; the tensor
                 // map clips the ragged edges.  One staging buffer per warp: before refilling it the
