@@ -134,6 +134,14 @@ typedef struct tl_gemm_solution {
  * are loaded (the tuned-solution database that replaces the reference's Tensile LibraryLogic yaml,
  * test/work/tensile tune). */
 TL_API tl_status tl_init(tl_handle** handle);
+/* A planning handle for a described device, made without any CUDA call and holding no device
+ * memory: sm_count SMs, smem_optin bytes of opt-in shared memory per block, and clusters4 clusters
+ * of four CTAs (one per SM) resident at once (0: sm_count / 4; a GB300 runs 36 on its 152 SMs).
+ * Only tl_default_solution, tl_check_solution, tl_device_info (compute capability 10.3),
+ * tl_load_solutions, tl_launch_count, tl_set_wait_timeout and tl_destroy accept it; calls that launch,
+ * allocate or time work return TL_ERR_INVALID_ARG.  For offline planning and tests on hosts without
+ * a GPU; no counterpart in the reference (its solver needs the device). */
+TL_API tl_status tl_init_host(int sm_count, size_t smem_optin, int clusters4, tl_handle** handle);
 TL_API tl_status tl_destroy(tl_handle* handle);
 /* Message of the last failing call on this host thread ("" if none). */
 TL_API const char* tl_last_error_string(void);

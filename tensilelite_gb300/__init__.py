@@ -132,7 +132,8 @@ def lib():
     P, S = ctypes.POINTER(Problem), ctypes.POINTER(Solution)
     i64, i32, f32 = ctypes.c_int64, ctypes.c_int, ctypes.c_float
     sig = {
-        "tl_init": [ctypes.POINTER(_vp)], "tl_destroy": [_vp], "tl_device_info": [_vp, ctypes.POINTER(i32),
+        "tl_init": [ctypes.POINTER(_vp)], "tl_init_host": [i32, ctypes.c_size_t, i32, ctypes.POINTER(_vp)],
+        "tl_destroy": [_vp], "tl_device_info": [_vp, ctypes.POINTER(i32),
         ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_size_t)],
         "tl_problem_init": [P, i32, i32, i32, i32, i64, i64, i64],
         "tl_default_solution": [_vp, P, S], "tl_check_solution": [_vp, P, S],
@@ -242,6 +243,16 @@ class Handle:
         h = _vp()
         check(lib().tl_init(ctypes.byref(h)))
         self._h = h
+
+    @classmethod
+    def planning(cls, sm_count=152, smem_optin=232448, clusters4=36):
+        """A planning handle for a described device (tl_init_host; defaults: a GB300): solution
+        heuristics and legality checks without a GPU.  Calls that launch, allocate or time work raise."""
+        self = cls.__new__(cls)
+        h = _vp()
+        check(lib().tl_init_host(sm_count, smem_optin, clusters4, ctypes.byref(h)))
+        self._h = h
+        return self
 
     def close(self):
         if getattr(self, "_h", None):

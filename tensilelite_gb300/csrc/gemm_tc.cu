@@ -377,9 +377,11 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
         const int64_t R = rem * kp.num_kb;
         const int64_t Wmax = std::min<int64_t>(std::min<int64_t>(workers, 8 * rem), R / 2);
         // tail_split -1 asks for the balanced split whatever the piece length
-        const bool balanced = (L.tail_split == -1 || (L.tail_split == 0 && R / Wmax >= 48)) && L.promote_k == 0 &&
-                              Wmax >= rem && Wmax > 1;
-        if (balanced && L.workspace && rem > 0) {
+        // (the piece length R / Wmax is only formed once Wmax > 1: no whole last wave, or a single
+        // tile of one k-block, leaves Wmax at 0)
+        const bool balanced = rem > 0 && Wmax > 1 && Wmax >= rem && L.promote_k == 0 &&
+                              (L.tail_split == -1 || (L.tail_split == 0 && R / Wmax >= 48));
+        if (balanced && L.workspace) {
             // balanced split (automatic, long k): the k-blocks of the last partial wave's tiles
             // are cut into equal contiguous ranges, one per worker (at most 8 pieces per tile); a
             // range covers at most two tiles.  The pieces run first so their reductions overlap

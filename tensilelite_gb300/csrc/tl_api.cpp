@@ -48,6 +48,10 @@ struct tl_handle {
     size_t tev_used = 0;           // events recorded since the last fold
     double timing_ms = 0.0;
     int64_t timing_count = 0;
+    // A planning handle (tl_init_host): a described device, no CUDA context use and no device
+    // memory; only the planning calls accept it.
+    bool host_only = false;
+    int host_clusters4 = 0;        // clusters of 4 CTAs the described device runs at once (0: sm_count / 4)
 };
 
 struct tl_grouped_plan {
@@ -222,7 +226,8 @@ double tc_cost(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solut
     const int64_t tiles = ((p.n + kTcTileN * cg - 1) / (kTcTileN * cg)) * ((p.m + bm - 1) / bm) * p.batch;
     // real devices: the co-resident cluster count (clusters of 4 leave some SMs idle)
     const int64_t workers = std::max<int64_t>(
-        1, h->d_err ? tc_workers(in_dtype, p.dtype_d, cg, bm, s.stages, h->sm_count) : h->sm_count / cg);
+        1, h->d_err ? tc_workers(in_dtype, p.dtype_d, cg, bm, s.stages, h->sm_count)
+                    : (cg == 4 && h->host_clusters4 > 0 ? h->host_clusters4 : h->sm_count / cg));
     const int64_t split = std::max<int64_t>(1, s.split_k);
     const int64_t units = tiles * split;
     // per k-block and CTA: the MMA issue time (4 MMAs; about 500 clocks for any width up to 128
@@ -248,8 +253,8 @@ double tc_cost(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solut
         const int64_t Wb = std::min<int64_t>(std::min<int64_t>(workers, 8 * rem), R / 2);
         int64_t S = std::min<int64_t>(std::min<int64_t>(workers / rem, num_kb / 16), 8);
         if (s.tail_split > 1) S = std::min<int64_t>(s.tail_split, num_kb);
-        if (split == 1 && (s.tail_split == -1 || (s.tail_split == 0 && R / Wb >= 48)) && s.promote_k == 0 &&
-            Wb >= rem && Wb > 1) {
+        if (split == 1 && Wb > 1 && Wb >= rem && s.promote_k == 0 &&
+            (s.tail_split == -1 || (s.tail_split == 0 && R / Wb >= 48))) {
             // balanced split of the last partial wave (reduction exposed without a whole wave after)
             cost += unit_time(std::ceil(static_cast<double>(R) / Wb), static_cast<double>(workers * cg)) +
                     (full >= 1 ? 1000.0 : 3000.0 + epi);
@@ -871,6 +876,13 @@ TL_API const char* tl_status_string(tl_status st)
 
 TL_API int tl_version(void) { return 10000; }
 
+namespace {
+tl_status host_only_refused()
+{
+    return fail(TL_ERR_INVALID_ARG, "planning handle (tl_init_host): it cannot launch, allocate or time work");
+}
+}  // namespace
+
 TL_API tl_status tl_init(tl_handle** handle)
 {
     if (!handle) return fail(TL_ERR_INVALID_ARG, "handle out-pointer is NULL");
@@ -904,9 +916,34 @@ TL_API tl_status tl_init(tl_handle** handle)
     return TL_SUCCESS;
 }
 
+TL_API tl_status tl_init_host(int sm_count, size_t smem_optin, int clusters4, tl_handle** handle)
+{
+    if (!handle) return fail(TL_ERR_INVALID_ARG, "handle out-pointer is NULL");
+    *handle = nullptr;
+    if (sm_count < 1 || sm_count > 4096) return fail(TL_ERR_INVALID_ARG, "sm_count out of range");
+    if (smem_optin < 16 * 1024 || smem_optin > 1024 * 1024) return fail(TL_ERR_INVALID_ARG, "smem_optin out of range");
+    if (clusters4 < 0 || clusters4 > sm_count / 4) return fail(TL_ERR_INVALID_ARG, "clusters4 out of range");
+    tl_handle* h = new (std::nothrow) tl_handle();
+    if (!h) return fail(TL_ERR_ALLOC, "handle allocation failed");
+    h->device = -1;
+    h->sm_count = sm_count;
+    h->cc_major = 10;
+    h->cc_minor = 3;
+    h->smem_optin = smem_optin;
+    h->host_only = true;
+    h->host_clusters4 = clusters4;
+    snprintf(h->name, sizeof(h->name), "host description (%d SMs)", sm_count);
+    *handle = h;
+    return TL_SUCCESS;
+}
+
 TL_API tl_status tl_destroy(tl_handle* h)
 {
     if (!h) return TL_SUCCESS;
+    if (h->host_only) {
+        delete h;
+        return TL_SUCCESS;
+    }
     cudaDeviceSynchronize();
     if (h->ws) cudaFree(h->ws);
     if (h->counters) cudaFree(h->counters);
@@ -985,6 +1022,7 @@ TL_API tl_status tl_check_solution(tl_handle* h, const tl_gemm_problem* p, const
 TL_API tl_status tl_gemm(tl_handle* h, const tl_gemm_problem* p, const tl_gemm_solution* s, void* D, const void* C,
                          const void* A, const void* B, void* stream)
 {
+    if (h && h->host_only) return host_only_refused();
     if (!h) return fail(TL_ERR_INVALID_ARG, "handle is NULL");
     Prepared P;
     t_capturing = stream_capturing(S(stream));
@@ -1027,6 +1065,7 @@ static uint64_t tn_extent(uint64_t rows, uint64_t cols, uint64_t ld, uint64_t ba
 TL_API tl_status tl_tensile_launch(tl_handle* h, const char* kernel_name, const void* kernarg, size_t kernarg_bytes,
                                    void* stream)
 {
+    if (h && h->host_only) return host_only_refused();
     if (!h || !kernel_name || !kernarg) return fail(TL_ERR_INVALID_ARG, "NULL argument");
     if (kernarg_bytes < TL_TENSILE_KERNARG_BYTES)
         return fail(TL_ERR_INVALID_ARG, "Tensile argument buffer shorter than 148 bytes");
@@ -1090,6 +1129,7 @@ TL_API tl_status tl_tensile_launch(tl_handle* h, const char* kernel_name, const 
 TL_API tl_status tl_gemm_ex(tl_handle* h, const tl_gemm_problem* p, const tl_epilogue* epi,
                             const tl_gemm_solution* s, void* D, const void* C, const void* A, const void* B, void* stream)
 {
+    if (h && h->host_only) return host_only_refused();
     if (!h) return fail(TL_ERR_INVALID_ARG, "handle is NULL");
     if (!epi) return tl_gemm(h, p, s, D, C, A, B, stream);
     if (epi->activation < TL_ACT_NONE || epi->activation > TL_ACT_SILU)
@@ -1121,6 +1161,7 @@ TL_API tl_status tl_tune(tl_handle* h, const tl_gemm_problem* p, void* D, const 
                          const void* B, int max_candidates, int reps, const char* cache_path, tl_gemm_solution* best,
                          float* best_ms)
 {
+    if (h && h->host_only) return host_only_refused();
     if (!h || !best) return fail(TL_ERR_INVALID_ARG, "NULL argument");
     tl_status st = validate(p);
     if (st != TL_SUCCESS) return st;
@@ -1211,6 +1252,7 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
                                         const void* const* C, const void* const* A, const void* const* B,
                                         const tl_gemm_solution* sol, tl_grouped_plan** plan)
 {
+    if (h && h->host_only) return host_only_refused();
     if (!h || !probs || !plan || count < 1 || !D || !A || !B) return fail(TL_ERR_INVALID_ARG, "NULL argument or count < 1");
     *plan = nullptr;
     const tl_gemm_problem& p0 = probs[0];
@@ -1386,6 +1428,7 @@ TL_API tl_status tl_grouped_plan_info(const tl_grouped_plan* pl, double* flops, 
 TL_API tl_status tl_gemm_grouped(tl_handle* h, const tl_gemm_problem* probs, int count, void* const* D,
                                  const void* const* C, const void* const* A, const void* const* B, void* stream)
 {
+    if (h && h->host_only) return host_only_refused();
     tl_grouped_plan* pl = nullptr;
     tl_status st = tl_grouped_plan_create(h, probs, count, D, C, A, B, nullptr, &pl);
     if (st != TL_SUCCESS) return st;
@@ -1402,6 +1445,7 @@ TL_API tl_status tl_tune_grouped(tl_handle* h, const tl_gemm_problem* probs, int
                                  const void* const* C, const void* const* A, const void* const* B, int reps,
                                  tl_gemm_solution* best, float* best_ms)
 {
+    if (h && h->host_only) return host_only_refused();
     if (!h || !best || count < 1) return fail(TL_ERR_INVALID_ARG, "NULL argument");
     if (reps <= 0) reps = 5;
     cudaStream_t s;
@@ -1482,6 +1526,7 @@ TL_API tl_status tl_graph_capture_grouped(tl_grouped_plan* pl, void* stream, tl_
 TL_API tl_status tl_graph_capture_gemm(tl_handle* h, const tl_gemm_problem* p, const tl_gemm_solution* sol, void* D,
                                        const void* C, const void* A, const void* B, void* stream, tl_graph** out)
 {
+    if (h && h->host_only) return host_only_refused();
     if (!h || !out || !stream) return fail(TL_ERR_INVALID_ARG, "NULL argument (capture needs a non-default stream)");
     Prepared P;
     tl_status st = prepare(h, p, sol, D, C, A, B, &P);   // allocations happen before capture
@@ -1514,6 +1559,7 @@ TL_API tl_status tl_graph_destroy(tl_graph* g)
 TL_API tl_status tl_quantize_fp8(tl_handle* h, tl_dtype src_dtype, const void* src, int64_t n, void* dst,
                                  float* scale_out, float* amax_out, void* stream)
 {
+    if (h && h->host_only) return host_only_refused();
     if (!h || (!src && n) || (!dst && n) || n < 0) return fail(TL_ERR_INVALID_ARG, "bad argument");
     if (src_dtype != TL_DTYPE_FP32 && src_dtype != TL_DTYPE_FP16 && src_dtype != TL_DTYPE_BF16)
         return fail(TL_ERR_UNSUPPORTED, "quantize: source must be fp32, fp16 or bf16");
@@ -1525,6 +1571,7 @@ TL_API tl_status tl_quantize_fp8(tl_handle* h, tl_dtype src_dtype, const void* s
 
 TL_API tl_status tl_split_bf16x2(tl_handle* h, const float* src, int64_t n, void* hi, void* lo, void* stream)
 {
+    if (h && h->host_only) return host_only_refused();
     if (!h || n < 0 || (n && (!src || !hi || !lo))) return fail(TL_ERR_INVALID_ARG, "bad argument");
     return aux_split_bf16(src, n, 1, n, 1, n, static_cast<uint16_t*>(hi), static_cast<uint16_t*>(lo), nullptr,
                           S(stream), &h->launches);
@@ -1534,6 +1581,7 @@ TL_API tl_status tl_split_bf16x2(tl_handle* h, const float* src, int64_t n, void
 TL_API tl_status tl_error_norms(tl_handle* h, tl_dtype dtype_d, const void* D, int64_t ldd, const double* R,
                                 const double* W, int64_t ldr, int64_t m, int64_t n, double out[3], void* stream)
 {
+    if (h && h->host_only) return host_only_refused();
     if (!h || !out || m < 0 || n < 0 || ldd < m || ldr < m) return fail(TL_ERR_INVALID_ARG, "bad argument");
     if (dtype_bytes(dtype_d) == 0) return fail(TL_ERR_INVALID_ARG, "bad dtype");
     tl_status st = aux_error_norms(dtype_d, D, ldd, R, W, ldr, m, n, h->d_norms, S(stream), &h->launches);
@@ -1668,6 +1716,7 @@ TL_API tl_status tl_timer_destroy(tl_timer* t)
 
 TL_API tl_status tl_set_kernel_timing(tl_handle* h, int enable)
 {
+    if (h && h->host_only) return host_only_refused();
     if (!h) return fail(TL_ERR_INVALID_ARG, "handle is NULL");
     std::lock_guard<std::mutex> lock(h->mu);
     if (enable && h->tev.empty()) {
@@ -1695,6 +1744,7 @@ TL_API tl_status tl_set_kernel_timing(tl_handle* h, int enable)
 
 TL_API tl_status tl_kernel_timing(tl_handle* h, double* total_ms, int64_t* launches, int reset)
 {
+    if (h && h->host_only) return host_only_refused();
     if (!h) return fail(TL_ERR_INVALID_ARG, "handle is NULL");
     std::lock_guard<std::mutex> lock(h->mu);
     tl_status st = timing_fold(h);
@@ -1717,6 +1767,7 @@ TL_API tl_status tl_launch_count(tl_handle* h, int64_t* n)
 
 TL_API tl_status tl_device_status(tl_handle* h, void* stream)
 {
+    if (h && h->host_only) return host_only_refused();
     if (!h) return fail(TL_ERR_INVALID_ARG, "handle is NULL");
     cudaError_t e = cudaStreamSynchronize(S(stream));
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
