@@ -172,3 +172,17 @@ def test_single_tile_single_k_block_plans(gb300, m, n, k):
         s = gb300.default_solution(p)
         assert s.split_k == 1
         gb300.check_solution(p, s)
+
+
+def test_mn_major_rules(gb300):
+    # MN-major A (problem NN: A stored m-contiguous) is staged in 128-byte chunks of m per CTA
+    fp8_nn = Problem.make(520, 600, 704, dtype="fp8")
+    with pytest.raises(TLError) as e:     # a pair of 128 m rows leaves 64 fp8 rows (half a chunk) per CTA
+        gb300.check_solution(fp8_nn, _sol(macro_tile0=128, depth_u=128))
+    assert e.value.status == tl.ERR_UNSUPPORTED
+    gb300.check_solution(fp8_nn, _sol(macro_tile0=256, depth_u=128))
+    gb300.check_solution(Problem.make(520, 600, 704, dtype="fp8", trans_a=True), _sol(macro_tile0=128, depth_u=128))
+    with pytest.raises(TLError) as e:     # two pairs: each CTA needs two 128-byte chunks of m
+        gb300.check_solution(fp8_nn, _sol(macro_tile0=256, macro_tile1=512, depth_u=128))
+    assert e.value.status == tl.ERR_UNSUPPORTED
+    gb300.check_solution(Problem.make(520, 600, 704, dtype="bf16"), _sol(macro_tile0=256, macro_tile1=512))
