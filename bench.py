@@ -662,6 +662,11 @@ def run_grouped(args, w, name):
                          "unit": "TFLOP/s", "frac": round(value / max(world, 1) / peaks["bf16_tflops"], 4),
                          "traffic": None, "peak_source": peaks["source"] + " bf16 burst", "kernel_ms": round(kernel_ms, 6)},
             "clocks": clocks.summary(mark0, mark1), "gpu_launches": h.launch_count() - l0 or args.steps}
+    traffic = profile_traffic(f"tc_gemm_bf16_{name}")
+    if traffic:
+        alg = sum((m * k + k * n + m * n) * 2 for m, n, k in sizes)     # bf16 A, B and D (beta 0)
+        line["roofline"]["traffic"] = traffic
+        line["roofline"]["traffic_vs_algorithmic"] = round(traffic / alg, 3)
     if e2e:
         line["e2e"] = e2e
     if rank == 0 and not args.no_cpu:
