@@ -16,8 +16,12 @@ cast to bf16 (RNE), fp32 accumulation, bf16 output.  One step = one GEMM launch.
 
 Other workloads (--workload): fp16_4096_nn|nt|tn, bf16_4096_nt|tn, bf16_480x1024x4096, bf16x3_8192,
 simt_fp32_8192, fp8_8192, grouped256, fwdbwd.  `--impl reference` times the reference's CPU loop
-(the oracle port) on the same workload instead.  Multi-GPU (torchrun): every rank runs its own
-replica of the workload; value sums the ranks' FLOPs over the slowest rank's time.
+(the oracle port) on the same workload instead.
+
+One GPU only.  The library is a single-device GEMM (the reference has no multi-device path either),
+and its cluster-of-four kernel loads through TMA multicast, which is kept to one-GPU runs.  Launched
+with WORLD_SIZE > 1 (torchrun), the GPU arm prints one line saying so on rank 0 and every rank exits
+without touching a GPU; the reference arm (host cores only) runs on rank 0 alone.
 """
 from __future__ import annotations
 
@@ -240,55 +244,31 @@ def cpu_baseline(w, A, B, dtype, target_s=10.0, threads=None):
 
 
 # ----------------------------------------------------------------------------------------------
-# GPU arm
+# GPU arm (one GPU)
 # ----------------------------------------------------------------------------------------------
-def dist_setup(args):
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+def launch_env():
+    """(world size, rank) of a torchrun launch; (1, 0) for a plain one."""
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0"))
 
 
-def barrier(world):
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
+def smi_index():
+    """nvidia-smi's index of the GPU this process uses (device 0 of CUDA_VISIBLE_DEVICES)."""
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].strip()
+    return int(vis) if vis.isdigit() else 0
 
 
-def _reduce(x, op):
-    import torch
-    import torch.distributed as dist
-    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
-    t = torch.tensor([x], dtype=torch.float64, device=dev)
-    dist.all_reduce(t, op=op)
-    return float(t.item())
-
-
-def max_over_ranks(x, world):
-    """The slowest rank's time (every rank ran its replica of the workload)."""
-    if world == 1:
-        return x
-    import torch.distributed as dist
-    return _reduce(x, dist.ReduceOp.MAX)
-
-
-def sum_over_ranks(x, world):
-    """The work all ranks did together."""
-    if world == 1:
-        return x
-    import torch.distributed as dist
-    return _reduce(x, dist.ReduceOp.SUM)
+def refusal_line(world, impl):
+    return {"metric": METRIC, "impl": impl, "n_gpus": world,
+            "unavailable": f"one-GPU library: bench.py runs the GPU arm on one GPU only (asked for {world}); "
+                           "the library has no multi-device path and its cluster-of-four kernel uses TMA multicast, "
+                           "which is kept to one-GPU runs"}
 
 
 def run_gpu(args, w, name):
     import torch
     import tensilelite_gb300 as tl
 
-    world, rank, local = dist_setup(args)
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    torch.cuda.set_device(0)
     h = tl.Handle()
     dtype = w["dtype"]
     m, n, k = w["m"], w["n"], w["k"]
@@ -339,7 +319,7 @@ def run_gpu(args, w, name):
     torch.cuda.synchronize()
 
     flops = 2.0 * m * n * k
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(smi_index())
     clocks.start()
     with torch.cuda.stream(stream):
         for i in range(args.warmup):
@@ -348,7 +328,6 @@ def run_gpu(args, w, name):
     stream.synchronize()
     h.device_status(stream)
     time.sleep(0.2)
-    barrier(world)
     torch.cuda.synchronize()
     mark0 = clocks.mark()
     launches0 = h.launch_count()
@@ -369,13 +348,10 @@ def run_gpu(args, w, name):
     t_wall = time.perf_counter() - t_wall
     launches = h.launch_count() - launches0
     mark1 = clocks.mark()
-    barrier(world)
     h.device_status(stream)
     ms_total = ev0.elapsed_time(ev1)
-    ms_max = max_over_ranks(ms_total, world)
-    total_flops = sum_over_ranks(flops * args.steps, world)
-    value = total_flops / (ms_max / 1e3) / 1e12
-    ms_per_step = ms_max / args.steps
+    value = flops * args.steps / (ms_total / 1e3) / 1e12
+    ms_per_step = ms_total / args.steps
     kernel_ms = ms_total / args.steps
     if multi:
         kms, kn = h.kernel_timing(reset=True)
@@ -384,7 +360,7 @@ def run_gpu(args, w, name):
 
     # accuracy of the benchmarked result against an FP64 host oracle (numpy float64 matmul)
     err = None
-    if args.check and m * n * k <= 8192 ** 3 and rank == 0:
+    if args.check and m * n * k <= 8192 ** 3:
         a, b, c, d = sets[(args.steps - 1) % nsets]
         try:
             err = fp64_error(h, w, A, B, C, d, out_dt, scale_a, scale_b, base)
@@ -394,7 +370,7 @@ def run_gpu(args, w, name):
     # e2e through the public API: pinned host buffers in, result out, every step
     e2e = None
     if args.e2e_steps > 0:
-        e2e = run_e2e(h, p, sol, base, dC, m, n, tdt, stream, args.e2e_steps, world)
+        e2e = run_e2e(h, p, sol, base, dC, m, n, tdt, stream, args.e2e_steps)
     clocks.stop()
     clk = clocks.summary(mark0, mark1)
     peaks = load_peaks()
@@ -402,7 +378,7 @@ def run_gpu(args, w, name):
     # tensor work actually executed: the split paths run nterms bf16 products per output
     achieved = nterms * flops / (kernel_ms / 1e3) / 1e12
     line = {
-        "metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+        "metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 6), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": dtype,
         "data": f"synthetic: numpy PCG64 seed {w['seed']}, {'N(0,1)' if w['dist'] == 'normal' else 'uniform[-1,1)'}",
@@ -410,7 +386,7 @@ def run_gpu(args, w, name):
                    "beta": w["beta"], "kernel": kernel, "solution": sol.as_dict(),
                    "l2": f"rotating {nsets} input sets of {bytes_per_set / 2**20:.0f} MiB (> L2 together)"
                    if nsets > 1 else "inputs larger than L2",
-                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+                   "parallelism": "1 GPU"},
         "roofline": {"bound": "tensor" if kernel != "simt" else "fp32-pipe", "achieved": round(achieved, 2),
                      "peak": (peaks["bf16_tflops"] * (2 if dtype == "fp8" else 1)) if kernel != "simt"
                      else round(nominal_fp32_tflops(), 1),
@@ -436,10 +412,10 @@ def run_gpu(args, w, name):
         line["accuracy_vs_fp64"] = err
     if e2e is not None:
         line["e2e"] = e2e
-    if rank == 0 and not args.no_cpu:
+    if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(w, A, B, dtype, target_s=args.cpu_seconds)
     h.close()
-    return line if rank == 0 else None
+    return line
 
 
 def nominal_fp32_tflops():
@@ -491,7 +467,7 @@ def fp64_error(h, w, A, B, C, d, out_dt, scale_a, scale_b, base):
             "reduction": "on-device FP64 (tl_error_norms); reference = numpy float64 matmul of the exact operands"}
 
 
-def run_e2e(h, p, sol, base, dC, m, n, tdt, stream, steps, world):
+def run_e2e(h, p, sol, base, dC, m, n, tdt, stream, steps):
     """The GEMM through the public API with host buffers, pipelined over three streams: step i's
     operands go host->device (tl_memcpy_h2d) while step i-1 computes (tl_gemm) and step i-2's result
     goes device->host (tl_memcpy_d2h); device buffers are double-buffered and every hand-over is an
@@ -540,7 +516,6 @@ def run_e2e(h, p, sol, base, dC, m, n, tdt, stream, steps, world):
     for i in range(4):
         step(i)
     torch.cuda.synchronize()
-    barrier(world)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(s_in)
     for i in range(steps):
@@ -548,8 +523,8 @@ def run_e2e(h, p, sol, base, dC, m, n, tdt, stream, steps, world):
     s_in.wait_stream(s_out)
     ev1.record(s_in)
     ev1.synchronize()
-    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
-    flops = sum_over_ranks(p.flops() * steps, world)
+    ms = ev0.elapsed_time(ev1)
+    flops = p.flops() * steps
     return {"value": round(flops / (ms / 1e3) / 1e12, 3), "unit": "TFLOP/s", "h2d_bytes_per_step": int(bi),
             "d2h_bytes_per_step": int(bo), "steps": steps, "ms_per_step": round(ms / steps, 4),
             "path": "pinned host -> tl_memcpy_h2d -> tl_gemm -> tl_memcpy_d2h, three streams pipelined "
@@ -570,11 +545,7 @@ def run_grouped(args, w, name):
     CUDA graph; one step = one replay.  Entries N(0,1) from torch's generator seeded 3 on the device."""
     import torch
     import tensilelite_gb300 as tl
-    world, rank, local = dist_setup(args)
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    torch.cuda.set_device(0)
     h = tl.Handle()
     sizes = grouped_sizes(w["seed"], w["count"])
     gen = torch.Generator(device="cuda").manual_seed(w["seed"])
@@ -592,13 +563,12 @@ def run_grouped(args, w, name):
     plan = h.grouped_plan(probs, D, None, A, B, solution=sol)
     stream = torch.cuda.Stream()
     graph = plan.capture(stream)
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(smi_index())
     clocks.start()
     for _ in range(args.warmup):
         graph.launch(stream)
     stream.synchronize()
     h.device_status(stream)
-    barrier(world)
     mark0 = clocks.mark()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = h.launch_count()
@@ -609,8 +579,8 @@ def run_grouped(args, w, name):
     ev1.synchronize()
     mark1 = clocks.mark()
     h.device_status(stream)
-    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
-    value = sum_over_ranks(flops * args.steps, world) / (ms / 1e3) / 1e12
+    ms = ev0.elapsed_time(ev1)
+    value = flops * args.steps / (ms / 1e3) / 1e12
     # e2e: host operands in, results out, through the public API (plan launch), every step
     e2e = None
     if args.e2e_steps > 0:
@@ -640,8 +610,8 @@ def run_grouped(args, w, name):
             step()
         e1.record(stream)
         e1.synchronize()
-        ems = max_over_ranks(e0.elapsed_time(e1), world)
-        e2e = {"value": round(sum_over_ranks(flops * esteps, world) / (ems / 1e3) / 1e12, 3),
+        ems = e0.elapsed_time(e1)
+        e2e = {"value": round(flops * esteps / (ems / 1e3) / 1e12, 3),
                "unit": "TFLOP/s", "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo),
                "steps": esteps, "path": "pinned host -> tl_memcpy_h2d x512 -> tl_grouped_plan_launch -> "
                                                  "tl_memcpy_d2h x256, one stream"}
@@ -649,7 +619,7 @@ def run_grouped(args, w, name):
     peaks = load_peaks()
     fl, tiles, psol = plan.info()
     kernel_ms = ms / args.steps
-    line = {"metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(kernel_ms, 6), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16",
             "data": f"synthetic: sizes numpy PCG64 seed {w['seed']}; entries N(0,1) torch CUDA generator seed {w['seed']}",
@@ -657,9 +627,9 @@ def run_grouped(args, w, name):
                                    f"one persistent launch replayed from a CUDA graph",
                        "problems": w["count"], "total_flop": flops, "tiles": tiles, "solution": psol.as_dict(),
                        "tuned_ms": round(tuned_ms, 4), "l2": f"operands {sum(a.numel() + b.numel() for a, b in zip(A, B)) * 2 / 2**30:.1f} GiB > L2",
-                       "parallelism": "replicas" if world > 1 else "1 GPU"},
-            "roofline": {"bound": "tensor", "achieved": round(value / max(world, 1), 2), "peak": peaks["bf16_tflops"],
-                         "unit": "TFLOP/s", "frac": round(value / max(world, 1) / peaks["bf16_tflops"], 4),
+                       "parallelism": "1 GPU"},
+            "roofline": {"bound": "tensor", "achieved": round(value, 2), "peak": peaks["bf16_tflops"],
+                         "unit": "TFLOP/s", "frac": round(value / peaks["bf16_tflops"], 4),
                          "traffic": None, "peak_source": peaks["source"] + " bf16 burst", "kernel_ms": round(kernel_ms, 6)},
             "clocks": clocks.summary(mark0, mark1), "gpu_launches": h.launch_count() - l0 or args.steps}
     traffic = profile_traffic(f"tc_gemm_bf16_{name}")
@@ -669,7 +639,7 @@ def run_grouped(args, w, name):
         line["roofline"]["traffic_vs_algorithmic"] = round(traffic / alg, 3)
     if e2e:
         line["e2e"] = e2e
-    if rank == 0 and not args.no_cpu:
+    if not args.no_cpu:
         m, n, k = sizes[0]
         wl = dict(dtype="bf16", m=m, n=n, k=k, lay="NN", alpha=1.0, beta=0.0, seed=w["seed"], dist="normal")
         Ah = A[0].float().cpu().numpy()
@@ -680,7 +650,7 @@ def run_grouped(args, w, name):
     plan.close()
     graph.close()
     h.close()
-    return line if rank == 0 else None
+    return line
 
 
 def run_fwdbwd(args, w, name):
@@ -689,11 +659,7 @@ def run_fwdbwd(args, w, name):
     (torch.cuda.graph around the autograd calls) and replayed; eager: the same step called from Python."""
     import torch
     import tensilelite_gb300 as tl
-    world, rank, local = dist_setup(args)
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    torch.cuda.set_device(0)
     M, K, N = w["m"], w["k"], w["n"]
     g = np.random.default_rng(w["seed"])
     Xh = (g.standard_normal(M * K) * 0.02).astype(np.float32).reshape(M, K)
@@ -748,12 +714,11 @@ def run_fwdbwd(args, w, name):
     graph.replay()
     torch.cuda.synchronize()
     h.device_status()
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(smi_index())
     clocks.start()
     for _ in range(args.warmup):
         graph.replay()
     torch.cuda.synchronize()
-    barrier(world)
     mark0 = clocks.mark()
     ev0.record()
     for _ in range(args.steps):
@@ -762,8 +727,8 @@ def run_fwdbwd(args, w, name):
     ev1.synchronize()
     mark1 = clocks.mark()
     h.device_status()
-    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
-    value = sum_over_ranks(flops * args.steps, world) / (ms / 1e3) / 1e12
+    ms = ev0.elapsed_time(ev1)
+    value = flops * args.steps / (ms / 1e3) / 1e12
     # FP64 reference gradients at full size
     Xd, Wd, dYd = X.detach().double(), W.detach().double(), dY.double()
     err = {}
@@ -788,16 +753,16 @@ def run_fwdbwd(args, w, name):
             hdW.copy_(W.grad, non_blocking=True)
         e1.record()
         e1.synchronize()
-        ems = max_over_ranks(e0.elapsed_time(e1), world)
-        e2e = {"value": round(sum_over_ranks(flops * args.e2e_steps, world) / (ems / 1e3) / 1e12, 3),
+        ems = e0.elapsed_time(e1)
+        e2e = {"value": round(flops * args.e2e_steps / (ems / 1e3) / 1e12, 3),
                "unit": "TFLOP/s", "h2d_bytes_per_step": 2 * (M * K + K * N + M * N),
                "d2h_bytes_per_step": 2 * (M * K + K * N), "steps": args.e2e_steps,
                "path": "pinned host -> copy -> tensilelite_gb300.matmul fwd+bwd (eager) -> grads to pinned host"}
     clocks.stop()
     peaks = load_peaks()
     # the replayed graph is the three GEMM kernels back to back: its time is their summed duration
-    achieved = value / max(world, 1)
-    line = {"metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+    achieved = value
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 6), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
             "data": f"synthetic: numpy PCG64 seed {w['seed']}: X, W ~ N(0,1)*0.02, dY ~ N(0,1)",
@@ -806,7 +771,7 @@ def run_fwdbwd(args, w, name):
                        "eager": {"value": round(flops / (eager_ms / 1e3) / 1e12, 3), "ms_per_step": round(eager_ms, 6),
                                  "steps": eager_steps},
                        "l2": "operands 48 MiB: L2-resident between steps (no flush)",
-                       "parallelism": "replicas" if world > 1 else "1 GPU"},
+                       "parallelism": "1 GPU"},
             "roofline": {"bound": "tensor", "achieved": round(achieved, 2), "peak": peaks["bf16_tflops"],
                          "unit": "TFLOP/s", "frac": round(achieved / peaks["bf16_tflops"], 4),
                          "traffic": None, "peak_source": peaks["source"] + " bf16 burst",
@@ -818,22 +783,20 @@ def run_fwdbwd(args, w, name):
             "gpu_launches": int(round(eager_launches * args.steps))}
     if e2e:
         line["e2e"] = e2e
-    if rank == 0 and not args.no_cpu:
+    if not args.no_cpu:
         wl = dict(dtype="bf16", m=N, n=M, k=K, lay="NN", alpha=1.0, beta=0.0, seed=w["seed"], dist="normal")
         # Y^T = W^T X^T column-major: A = W's storage (N x K), B = X's storage (K x M)
         line["cpu_baseline"] = cpu_baseline(wl, W.detach().float().cpu().numpy().reshape(-1),
                                             X.detach().float().cpu().numpy().reshape(-1), "fp32",
                                             target_s=args.cpu_seconds)
-    return line if rank == 0 else None
+    return line
 
 
 # ----------------------------------------------------------------------------------------------
 # reference arm: the reference's CPU GEMM loop (oracle port), all host threads
 # ----------------------------------------------------------------------------------------------
 def run_reference(args, w, name):
-    world, rank, _ = dist_setup(args)
-    if rank != 0:
-        return None
+    world, _ = launch_env()
     from oracle import oracle as orc
     orc.lib()
     threads = os.cpu_count() or 1
@@ -888,6 +851,14 @@ def main():
     if args.steps is None:
         args.steps = w.get("steps", 10000)
     kind = w.get("kind", "gemm")
+    world, rank = launch_env()
+    if world > 1:
+        # the GPU arm is a one-GPU deliverable; the reference arm uses host cores on rank 0 only
+        if rank != 0:
+            return
+        if args.impl != "reference":
+            print(json.dumps(refusal_line(world, args.impl)), flush=True)
+            return
     if args.impl == "reference":
         if kind == "grouped":
             m, n, k = grouped_sizes(w["seed"], w["count"])[0]

@@ -101,7 +101,10 @@ typedef struct tl_gemm_problem {
  *   depth_u        k per pipeline stage (loop_unroll / -u)
  *   stages         shared-memory ring depth (lds_buffer_num / -f)
  *   wave_tile0/1   SIMT: outputs per thread along m / n;  TCGEN05: ignored
- * TCGEN05: macro_tile1 is the tcgen05 M extent (128, problem n maps to TMEM lanes) and
+ * TCGEN05: macro_tile1 is the tcgen05 M extent (128 on one SM, 256 on a CTA pair; problem n maps
+ * to TMEM lanes) or 512 (two CTA pairs sharing the m-side operand through a TMA multicast load,
+ * accepted only when A and B are memory of the current device, else TL_ERR_UNSUPPORTED; the
+ * heuristic falls back to a CTA pair) and
  * macro_tile0 is the tcgen05 N extent (64, 128, 192 or 256 along m); depth_u is fixed by the
  * input type (64 for 16-bit, 128 for fp8: one 128-byte swizzle row).  split_k > 1 divides k
  * across CTAs and reduces through a device workspace owned by the handle.
@@ -123,8 +126,16 @@ typedef struct tl_gemm_solution {
     int32_t tail_split;        /* split of a last, partial wave of tiles along k: 0 automatic,
                                   1 off, S >= 2 each of its tiles in S equal k-slices, -1 its
                                   k-blocks spread evenly over all workers (balanced) */
-    int32_t reserved[4];
+    int32_t debug_flags;       /* 0 for every real use; TL_DEBUG_SKIP_LOADS tests the timeout path */
+    int32_t reserved[3];
 } tl_gemm_solution;
+
+/* debug_flags bits (tensor-core kernels).  TL_DEBUG_SKIP_LOADS: the TMA producer issues no copies,
+ * so the MMA and epilogue waits run out their limit (tl_set_wait_timeout) and the call reports
+ * TL_ERR_TIMEOUT through tl_device_status / tl_noalloc_status instead of computing D.  It exists
+ * to test that a device wait that expires is reported and leaves the context usable; nothing is
+ * issued that could still be in flight when the kernel returns. */
+#define TL_DEBUG_SKIP_LOADS 1
 
 /* ---- handles and errors --------------------------------------------------------------------- */
 
@@ -177,7 +188,10 @@ TL_API tl_status tl_gemm(tl_handle* handle, const tl_gemm_problem* problem,
 
 /* Time candidate solutions on the given buffers (D is overwritten) and return the fastest in
  * `best`; the result is cached in the handle and, if `cache_path` is non-NULL, merged into that
- * JSON file keyed by device and problem.  Synchronous.  Replaces test/perf_test.py:58-167. */
+ * JSON file keyed by device and problem.  A candidate whose launches report a device error (a
+ * bounded wait that ran out) is dropped, never returned or cached.  When D == C with beta != 0 the
+ * candidates write a scratch output instead, so C is left intact.  Synchronous.  Replaces
+ * test/perf_test.py:58-167. */
 TL_API tl_status tl_tune(tl_handle* handle, const tl_gemm_problem* problem, void* D, const void* C,
                          const void* A, const void* B, int max_candidates, int reps,
                          const char* cache_path, tl_gemm_solution* best, float* best_ms);
@@ -255,9 +269,17 @@ TL_API tl_status tl_load_solutions(tl_handle* handle, const char* cache_path, in
  * process exits); problems whose workspace exceeds it are refused with TL_ERR_UNSUPPORTED.  All calls
  * share that array: each clears the parts it uses, and calls that overlap on the GPU race.  The
  * first call on a device looks the array up with that device current -- make it before any stream
- * capture.  fp16/bf16/fp8 operands (TCGEN05 only); solution == NULL uses the heuristic. */
+ * capture.  The call runs on the caller's current device and context (runtime API) and never
+ * changes them.  fp16/bf16/fp8 operands (TCGEN05 only); solution == NULL uses the heuristic.  A
+ * bounded device wait that runs out is recorded in the array's error word: read it with
+ * tl_noalloc_status. */
 TL_API tl_status tl_gemm_noalloc(const tl_gemm_problem* problem, const tl_gemm_solution* solution, void* D,
                                  const void* C, const void* A, const void* B, void* stream);
+/* Synchronise `stream` and read, then clear, the error word of the last tl_gemm_noalloc call on the
+ * current device (each call clears it when it starts): TL_SUCCESS, or TL_ERR_TIMEOUT when a device
+ * wait of that call ran out and D is not valid.  Allocates nothing.  No counterpart in the
+ * reference (its launches report through E_ReturnState, inc/ff_utils.h:44-50). */
+TL_API tl_status tl_noalloc_status(void* stream);
 
 /* ---- grouped GEMM (one persistent launch over many independent problems) ---------------------- */
 

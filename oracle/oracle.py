@@ -36,11 +36,14 @@ def build(quiet: bool = True) -> str:
     return os.path.join(_HERE, "liboracle.so")
 
 
-def build_ref() -> str | None:
-    """Compile the reference's converters from the reference tree, if it is present."""
-    ref = os.environ.get("TL_REFERENCE_TREE", "/root/reference")
+def build_ref(ref_tree: str | None = None) -> str | None:
+    """Compile the reference's converters from the reference tree: `ref_tree`, else the environment
+    variable TL_REFERENCE_TREE.  Raises when neither names a tree holding inc/ff_utils.h."""
+    ref = ref_tree or os.environ.get("TL_REFERENCE_TREE")
+    if not ref:
+        raise RuntimeError("the reference tree is not set: pass ref_tree or set TL_REFERENCE_TREE")
     if not os.path.isfile(os.path.join(ref, "inc", "ff_utils.h")):
-        return None
+        raise RuntimeError(f"no reference tree at {ref} (inc/ff_utils.h missing)")
     out = subprocess.run(["make", "-C", _HERE, "ref", "REF=" + ref], capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("reference converter build failed:\n" + out.stdout + out.stderr)

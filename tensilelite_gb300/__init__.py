@@ -33,6 +33,7 @@ FP32, FP16, BF16, FP8 = 1, 2, 3, 4
 OP_N, OP_T = 0, 1
 KERNEL_AUTO, KERNEL_SIMT, KERNEL_TCGEN05, KERNEL_BF16X3, KERNEL_BF16X6 = 0, 1, 2, 3, 4
 ROUND_RNE, ROUND_TRUNCATE = 0, 1
+DEBUG_SKIP_LOADS = 1   # tl_gemm_solution.debug_flags: the producer issues no copies (timeout-path tests)
 
 DTYPE_BYTES = {FP32: 4, FP16: 2, BF16: 2, FP8: 1}
 DTYPE_NAMES = {"fp32": FP32, "fp16": FP16, "bf16": BF16, "fp8": FP8, "fp8_e4m3": FP8}
@@ -108,7 +109,7 @@ class Solution(ctypes.Structure):
                 ("depth_u", ctypes.c_int32), ("stages", ctypes.c_int32), ("wave_tile0", ctypes.c_int32),
                 ("wave_tile1", ctypes.c_int32), ("split_k", ctypes.c_int32), ("raster", ctypes.c_int32),
                 ("ctas", ctypes.c_int32), ("promote_k", ctypes.c_int32),
-                ("tail_split", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
+                ("tail_split", ctypes.c_int32), ("debug_flags", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
@@ -169,6 +170,8 @@ def lib():
         "tl_tensile_launch": [_vp, ctypes.c_char_p, _vp, ctypes.c_size_t, _vp],
         "tl_kernel_timing": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(i64), i32],
         "tl_set_wait_timeout": [_vp, ctypes.c_uint32],
+        "tl_gemm_noalloc": [P, S, _vp, _vp, _vp, _vp, _vp],
+        "tl_noalloc_status": [_vp],
     }
     for name, argt in sig.items():
         fn = getattr(L, name)
@@ -435,6 +438,19 @@ class GroupedPlan:
             self.close()
         except Exception:
             pass
+
+
+def gemm_noalloc(p: Problem, D, C, A, B, solution: Optional[Solution] = None, stream=None):
+    """tl_gemm_noalloc: the tensor-core GEMM with its split-k scratch in the library's static device
+    array (no allocation, no handle)."""
+    check(lib().tl_gemm_noalloc(ctypes.byref(p), ctypes.byref(solution) if solution is not None else None,
+                                _ptr(D), _ptr(C), _ptr(A), _ptr(B), _stream_ptr(stream)))
+
+
+def noalloc_status(stream=None):
+    """tl_noalloc_status: raises TLError(ERR_TIMEOUT) when the last tl_gemm_noalloc call on the current
+    device ran out a device wait (and clears the record)."""
+    check(lib().tl_noalloc_status(_stream_ptr(stream)))
 
 
 _DEFAULT_HANDLE = {}

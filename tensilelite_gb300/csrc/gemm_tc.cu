@@ -449,6 +449,7 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     kp.counters = L.counters;
     kp.err = L.err;
     kp.timeout_ns = L.timeout_ns;
+    kp.debug_skip_loads = (L.debug_flags & TL_DEBUG_SKIP_LOADS) ? 1 : 0;
     st = dispatch(L.in_dtype, L.out_dtype, cg, kp, L.ctas, L.sm_count, kp.total_work, smem, stream);
     if (st == TL_SUCCESS && launches) ++*launches;
     return st;

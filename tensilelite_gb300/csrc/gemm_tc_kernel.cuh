@@ -66,6 +66,7 @@ struct TcKernelParams {
     int* counters;
     int* err;
     unsigned long long timeout_ns;
+    int debug_skip_loads;         // TL_DEBUG_SKIP_LOADS: the producer issues no copies (timeout-path test)
 };
 
 struct TileJob {
@@ -803,7 +804,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         ok = false;
                         break;
                     }
-                    if (ptx::elect_one()) {
+                    // the timeout-path test issues nothing: the full barriers never complete, the
+                    // MMA and epilogue waits run out, and no copy is left in flight
+                    if (!p.debug_skip_loads && ptx::elect_one()) {
                         uint8_t* sN = smem + static_cast<size_t>(stage) * stage_bytes;
                         uint8_t* sM = sN + tileN_bytes;
                         // split-precision products, smallest first (term table set by the host)

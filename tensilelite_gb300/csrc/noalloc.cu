@@ -15,8 +15,12 @@
 //     work overlaps on the GPU (different streams, no ordering between them) race on it.
 //   * The first call on a device looks up the array's device address (cudaGetSymbolAddress) with
 //     that device current; make that first call before any stream capture.
+//   * A kernel whose bounded wait ran out ORs a role mask into the error word and returns early;
+//     tl_noalloc_status reads and clears it (a device-to-host copy into a host int, no allocation).
+//   * Calls use the caller's current device and context; nothing here calls cudaSetDevice.
 #include <cuda_runtime.h>
 
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -77,22 +81,19 @@ using namespace tl;
 extern "C" TL_API tl_status tl_gemm_noalloc(const tl_gemm_problem* problem, const tl_gemm_solution* solution,
                                             void* D, const void* C, const void* A, const void* B, void* stream)
 {
+    // The caller's current device and context are used as they are (no cudaSetDevice): a caller on
+    // the driver API keeps its own current context.  The memset below is a runtime call on that
+    // context, so the tensor-map encoding after it always runs with a context current.
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
     if (dev < 0 || dev >= kMaxDevices) return fail(TL_ERR_UNSUPPORTED, "device ordinal beyond 63");
-    // bind the device's primary context to this thread (tensor-map encoding is a driver call)
-    static thread_local int bound = -1;
-    if (bound != dev) {
-        if ((e = cudaSetDevice(dev)) != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
-        bound = dev;
-    }
     NoallocDevice* nd = nullptr;
     tl_status st = noalloc_setup(dev, &nd);
     if (st != TL_SUCCESS) return st;
     TcLaunch L;
     size_t ws_bytes = 0, counters = 0;
-    st = plan_tc_noalloc(nd->sm_count, nd->smem_optin, problem, solution, D, C, A, B, &L, &ws_bytes, &counters);
+    st = plan_tc_noalloc(dev, nd->sm_count, nd->smem_optin, problem, solution, D, C, A, B, &L, &ws_bytes, &counters);
     if (st != TL_SUCCESS) return st;
     if (ws_bytes > kNoallocPartialBytes || counters > kNoallocCounters)
         return fail(TL_ERR_UNSUPPORTED,
@@ -118,4 +119,31 @@ extern "C" TL_API tl_status tl_gemm_noalloc(const tl_gemm_problem* problem, cons
         if (v > 0) L.timeout_ns = static_cast<uint64_t>(v) * 1000000ull;
     }
     return tc_gemm_launch(L, s, nullptr);
+}
+
+// The error word is the first int of the array; kernels that ran out a bounded wait OR a role mask
+// into it.  Read on `stream` (after the calls queued there) into a host int, then cleared.
+extern "C" TL_API tl_status tl_noalloc_status(void* stream)
+{
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) return fail(TL_ERR_UNSUPPORTED, "device ordinal beyond 63");
+    NoallocDevice* nd = nullptr;
+    tl_status st = noalloc_setup(dev, &nd);
+    if (st != TL_SUCCESS) return st;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int v = 0;
+    if ((e = cudaMemcpyAsync(&v, nd->scratch, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return cuda_fail(e, "cudaMemcpyAsync(noalloc error word)");
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    if (v != 0) {
+        if ((e = cudaMemsetAsync(nd->scratch, 0, sizeof(int), s)) != cudaSuccess)
+            return cuda_fail(e, "cudaMemsetAsync(noalloc error word)");
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+        char buf[128];
+        snprintf(buf, sizeof(buf), "tl_gemm_noalloc: device wait timed out (role mask 0x%x); D is not valid", v);
+        return fail(TL_ERR_TIMEOUT, buf);
+    }
+    return TL_SUCCESS;
 }

@@ -210,6 +210,34 @@ void simt_solution(tl_gemm_solution* s)
 bool m_mn_major(const tl_gemm_problem& p) { return p.trans_a == TL_OP_N; }   // A[m + k*lda]
 bool n_mn_major(const tl_gemm_problem& p) { return p.trans_b == TL_OP_T; }   // B[n + k*ldb]
 
+// Two CTA pairs per cluster (macro_tile1 512) load the shared m-side operand with a TMA multicast
+// copy.  That copy is kept to memory of the GPU running the kernel: an operand must be device (or
+// managed) memory of `device`, as cudaPointerGetAttributes reports it -- not host memory, another
+// GPU's memory or an unregistered pointer.
+bool on_device(const void* ptr, int device)
+{
+    if (!ptr) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) && a.device == device;
+}
+
+bool multicast_ok(const void* A, const void* B, int device) { return on_device(A, device) && on_device(B, device); }
+
+tl_status multicast_refused()
+{
+    return fail(TL_ERR_UNSUPPORTED,
+                "macro_tile1 512 (two CTA pairs sharing the m-side operand) uses a TMA multicast load, which this "
+                "library runs only on device memory of the current GPU; A or B is host memory, another device's "
+                "memory or not a CUDA allocation (use macro_tile1 256)");
+}
+
+// The heuristic's tile without the multicast variant: the same tile on a CTA pair.
+void drop_cluster4(const tl_handle* h, tl_gemm_solution* s);
+
 tl_status check_tc_solution(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solution& s);
 
 // Modelled duration of one tensor-core launch, in SM clocks.  Per 128-byte k-block a CTA needs its
@@ -377,7 +405,15 @@ tl_status check_tc_solution(const tl_handle* h, const tl_gemm_problem& p, const 
     if (s.tail_split < -1 || s.tail_split > 8) return fail(TL_ERR_INVALID_ARG, "tail_split must be in [-1, 8]");
     if (s.promote_k > 0 && bm != 128)
         return fail(TL_ERR_UNSUPPORTED, "promote_k needs macro_tile0 == 128 (fp32 running sums, TMEM budget)");
+    if (s.debug_flags & ~TL_DEBUG_SKIP_LOADS) return fail(TL_ERR_INVALID_ARG, "unknown debug_flags bit");
     return TL_SUCCESS;
+}
+
+void drop_cluster4(const tl_handle* h, tl_gemm_solution* s)
+{
+    if (s->macro_tile1 != 4 * kTcTileN) return;
+    s->macro_tile1 = 2 * kTcTileN;
+    s->stages = std::min(6, max_stages(s->macro_tile0 / 2, h->smem_optin));
 }
 
 std::string problem_key(const tl_handle* h, const tl_gemm_problem& p)
@@ -529,6 +565,12 @@ tl_status prepare(tl_handle* h, const tl_gemm_problem* prob, const tl_gemm_solut
         } else {
             return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel: " + why);
         }
+    }
+    // the multicast variant reads A and B only where they are this GPU's own memory: an explicit
+    // request is refused otherwise, a heuristic or tuned choice drops to the CTA pair
+    if (kernel == TL_KERNEL_TCGEN05 && has_work && P.s.macro_tile1 == 4 * kTcTileN && !multicast_ok(A, B, h->device)) {
+        if (sol) return multicast_refused();
+        drop_cluster4(h, &P.s);
     }
     P.kernel = kernel;
     if (kernel == TL_KERNEL_SIMT) {
@@ -707,6 +749,7 @@ tl_status enqueue(tl_handle* h, const Prepared& P, cudaStream_t s)
     L.epi_amax = P.epi.amax;
     L.epi_bias_dtype = P.epi.bias_dtype;
     L.epi_act = P.epi.activation;
+    L.debug_flags = P.s.debug_flags;
     const bool timed = timing_begin(h, s);
     const tl_status st = tc_gemm_launch(L, s, &h->launches);
     timing_end(h, s, timed, st);
@@ -790,9 +833,9 @@ tl_status save_cache(const char* path, const std::string& key, const tl_gemm_sol
 // Validation and launch description of a tcgen05 GEMM for a caller that supplies the scratch
 // itself (tl_gemm_noalloc).  Allocates nothing: it only checks the problem and the solution and
 // reports how much split-k workspace (bytes) and how many tile counters the launch needs.
-tl_status plan_tc_noalloc(int sm_count, size_t smem_optin, const tl_gemm_problem* prob, const tl_gemm_solution* sol,
-                          void* D, const void* C, const void* A, const void* B, TcLaunch* L, size_t* ws_bytes,
-                          size_t* counter_count)
+tl_status plan_tc_noalloc(int device, int sm_count, size_t smem_optin, const tl_gemm_problem* prob,
+                          const tl_gemm_solution* sol, void* D, const void* C, const void* A, const void* B,
+                          TcLaunch* L, size_t* ws_bytes, size_t* counter_count)
 {
     tl_status st = validate(prob);
     if (st != TL_SUCCESS) return st;
@@ -816,6 +859,10 @@ tl_status plan_tc_noalloc(int sm_count, size_t smem_optin, const tl_gemm_problem
         if (s.kernel != TL_KERNEL_TCGEN05) return fail(TL_ERR_UNSUPPORTED, "tl_gemm_noalloc: solution must be TCGEN05");
     } else {
         tc_heuristic(&dev, p, TL_KERNEL_TCGEN05, &s);
+    }
+    if (s.macro_tile1 == 4 * kTcTileN && p.m > 0 && p.n > 0 && p.k > 0 && !multicast_ok(A, B, device)) {
+        if (sol) return multicast_refused();
+        drop_cluster4(&dev, &s);
     }
     if ((st = check_tc_solution(&dev, p, s)) != TL_SUCCESS) return st;
     const int cgp = s.macro_tile1 / kTcTileN;
@@ -843,6 +890,7 @@ tl_status plan_tc_noalloc(int sm_count, size_t smem_optin, const tl_gemm_problem
     L->promote_k = s.promote_k;
     L->cg = cgp;
     L->tail_split = 1;     // the static scratch is sized for explicit split-k only
+    L->debug_flags = s.debug_flags;
     L->sm_count = sm_count;
     return TL_SUCCESS;
 }
@@ -1174,28 +1222,71 @@ TL_API tl_status tl_tune(tl_handle* h, const tl_gemm_problem* p, void* D, const 
     } else {
         cands = tc_candidates(h, *p, kernel);
     }
+    // the multicast variant only where A and B are this GPU's memory
+    if (!multicast_ok(A, B, h->device))
+        cands.erase(std::remove_if(cands.begin(), cands.end(),
+                                   [](const tl_gemm_solution& c) { return c.macro_tile1 == 4 * kTcTileN; }),
+                    cands.end());
     if (cands.empty()) return fail(TL_ERR_UNSUPPORTED, "no legal candidate solution");
     if (max_candidates <= 0) max_candidates = 16;
     if (reps <= 0) reps = 10;
     if (static_cast<int>(cands.size()) > max_candidates) cands.resize(max_candidates);
+    if ((st = bind_thread(h)) != TL_SUCCESS) return st;
+    // in place (D == C, beta != 0): every timed launch would fold beta*C into C again, so the
+    // candidates read C where it is and write a scratch output of D's extent instead
+    void* Dt = D;
+    void* scratch = nullptr;
+    if (D != nullptr && D == C && p->beta != 0.0f && p->m > 0 && p->n > 0) {
+        const size_t bytes = static_cast<size_t>(operand_span(p->ldd, p->n, p->batch, p->stride_d, p->m)) *
+                             dtype_bytes(p->dtype_d);
+        if (cudaMalloc(&scratch, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(TL_ERR_ALLOC, "tuner scratch output allocation failed");
+        }
+        Dt = scratch;
+    }
     cudaStream_t s;
-    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return fail(TL_ERR_CUDA, "stream create");
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+        if (scratch) cudaFree(scratch);
+        return fail(TL_ERR_CUDA, "stream create");
+    }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best_t = 1e30f;
     tl_gemm_solution best_s = cands[0];
     bool any = false;
+    std::string dropped;
+    // a candidate counts only if its launches finished without a device error: a bounded wait that
+    // ran out returns early and would look fastest
+    auto device_clean = [&](const tl_gemm_solution& c) {
+        int v = 0;
+        if (cudaStreamSynchronize(s) != cudaSuccess || cudaMemcpy(&v, h->d_err, sizeof(int), cudaMemcpyDeviceToHost) !=
+                                                           cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (v != 0) {
+            cudaMemset(h->d_err, 0, sizeof(int));
+            char buf[160];
+            snprintf(buf, sizeof(buf), " [mt %dx%d split %d: device wait timed out, mask 0x%x]", c.macro_tile0,
+                     c.macro_tile1, c.split_k, v);
+            dropped += buf;
+            return false;
+        }
+        return true;
+    };
     for (const auto& c : cands) {
         Prepared P;
-        if (prepare(h, p, &c, D, C, A, B, &P) != TL_SUCCESS) continue;
+        if (prepare(h, p, &c, Dt, C, A, B, &P) != TL_SUCCESS) continue;
         if (enqueue(h, P, s) != TL_SUCCESS) continue;          // warm-up
-        if (cudaStreamSynchronize(s) != cudaSuccess) { cudaGetLastError(); continue; }
+        if (!device_clean(c)) continue;
         cudaEventRecord(e0, s);
         bool ok = true;
         for (int r = 0; r < reps && ok; ++r) ok = enqueue(h, P, s) == TL_SUCCESS;
         cudaEventRecord(e1, s);
-        if (!ok || cudaEventSynchronize(e1) != cudaSuccess) continue;
+        if (!ok || cudaEventSynchronize(e1) != cudaSuccess) { cudaGetLastError(); continue; }
+        if (!device_clean(c)) continue;
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
         ms /= reps;
@@ -1205,7 +1296,8 @@ TL_API tl_status tl_tune(tl_handle* h, const tl_gemm_problem* p, void* D, const 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaStreamDestroy(s);
-    if (!any) return fail(TL_ERR_UNSUPPORTED, "every candidate failed: " + g_last_error);
+    if (scratch) cudaFree(scratch);
+    if (!any) return fail(TL_ERR_UNSUPPORTED, "every candidate failed: " + g_last_error + dropped);
     *best = best_s;
     if (best_ms) *best_ms = best_t;
     const std::string key = problem_key(h, *p);
@@ -1303,6 +1395,15 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
     s.kernel = TL_KERNEL_TCGEN05;
     if (s.split_k == 0) s.split_k = 1;
     if (s.split_k != 1) return fail(TL_ERR_UNSUPPORTED, "grouped GEMM does not split k");
+    if (s.macro_tile1 == 4 * kTcTileN) {
+        // the multicast variant only where every problem's A and B are this GPU's memory
+        bool local = true;
+        for (int i = 0; i < count && local; ++i) local = multicast_ok(A[i], B[i], h->device);
+        if (!local) {
+            if (sol) return multicast_refused();
+            drop_cluster4(h, &s);
+        }
+    }
     for (int i = 0; i < count; ++i)
         if ((st = check_tc_solution(h, probs[i], s)) != TL_SUCCESS) return st;
 
@@ -1775,6 +1876,9 @@ TL_API tl_status tl_device_status(tl_handle* h, void* stream)
     TL_CUDA_TRY(cudaMemcpy(&v, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
     if (v) {
         TL_CUDA_TRY(cudaMemset(h->d_err, 0, sizeof(int)));
+        // a launch that gave up may have left split-k arrival counters mid-count: the next launch
+        // expects them at zero
+        if (h->counters) TL_CUDA_TRY(cudaMemset(h->counters, 0, h->counters_len * sizeof(int)));
         char buf[128];
         snprintf(buf, sizeof(buf), "device wait timed out (role mask 0x%x)", v);
         return fail(TL_ERR_TIMEOUT, buf);

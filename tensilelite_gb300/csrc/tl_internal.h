@@ -99,6 +99,7 @@ struct TcLaunch {
     int epi_bias_dtype;
     int epi_act;
     int epi_on;
+    int debug_flags;         // tl_gemm_solution.debug_flags (TL_DEBUG_SKIP_LOADS)
 };
 
 // Dynamic shared memory of one CTA staging bm_cta m-rows per stage (bm / 2 for a CTA pair).
@@ -112,9 +113,9 @@ int tc_tmem_cols(int bm);
 tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launches);
 // Checks a tcgen05 GEMM and fills its launch description without allocating anything; the caller
 // provides err, workspace and counters (sizes reported in ws_bytes / counter_count).
-tl_status plan_tc_noalloc(int sm_count, size_t smem_optin, const tl_gemm_problem* prob, const tl_gemm_solution* sol,
-                          void* D, const void* C, const void* A, const void* B, TcLaunch* L, size_t* ws_bytes,
-                          size_t* counter_count);
+tl_status plan_tc_noalloc(int device, int sm_count, size_t smem_optin, const tl_gemm_problem* prob,
+                          const tl_gemm_solution* sol, void* D, const void* C, const void* A, const void* B,
+                          TcLaunch* L, size_t* ws_bytes, size_t* counter_count);
 
 // Grouped: build per-problem entries (host) and launch over a device table.
 struct TcGroupLaunch {

@@ -87,3 +87,54 @@ def quantize_out(vals_f32, out_dtype, rounding="rne"):
         return np.asarray(vals_f32, np.float32)
     bits = orc.encode(np.asarray(vals_f32, np.float32), out_dtype, bf16_rounding=rounding)
     return orc.decode(bits, out_dtype)
+
+
+# ---- the parity tolerance (both sides accumulate in fp32, in different orders) ----
+MANT = {"fp32": 23, "fp16": 10, "bf16": 7}
+
+
+def ulp_out(x, od):
+    mag = np.maximum(np.abs(x), {"fp32": 2.0 ** -126, "fp16": 2.0 ** -14, "bf16": 2.0 ** -126}[od])
+    return 2.0 ** (np.floor(np.log2(mag)) - MANT[od])
+
+
+def assert_close(G, R, absprod, k, alpha, beta, Cm, od, rounding="rne"):
+    """G: GPU result (m x n, exact fp32 values of the output), R: oracle fp32 result.  Truncating
+    output rounding may lose a whole ulp instead of half of one."""
+    G = np.asarray(G, np.float64)
+    R = np.asarray(R, np.float64)
+    bound = ulp_out(R, od) + 3.0 * k * 2.0 ** -24 * abs(alpha) * absprod
+    if beta != 0.0 and Cm is not None:
+        bound = bound + 2.0 ** -23 * np.abs(beta * np.asarray(Cm, np.float64))
+    err = np.abs(G - R)
+    bad = int(np.count_nonzero(err > bound))
+    assert np.all(np.isfinite(G)), "non-finite output"
+    assert bad == 0, f"{bad} elements beyond the bound; worst excess {float(np.max(err - bound)):.3e}"
+    nw = orc.normwise_error(G, R)
+    allowance = 2.0 ** -(MANT[od] + (0 if rounding == "trunc" else 1)) + 3.0 * k * 2.0 ** -24 * abs(alpha) * float(np.max(absprod)) / max(
+        float(np.max(np.abs(R))), 1e-30)
+    assert nw <= allowance, f"normwise {nw:.3e} > {allowance:.3e}"
+
+
+def absprod_of(case):
+    opA = orc.op_matrix(case["A"], case["trans_a"], case["m"], case["k"], case["lda"])
+    opB = orc.op_matrix(case["B"], case["trans_b"], case["k"], case["n"], case["ldb"])
+    return np.abs(opA) @ np.abs(opB)
+
+
+def check_against_oracle(got_flat, case, ldd=None, rounding="rne", n_begin=0, n_end=None, threads=8):
+    """Scores a GPU result (flat, exact fp32 values, leading dimension ldd) against the oracle's
+    restated reference loop on columns [n_begin, n_end) with the tolerance of assert_close."""
+    m, n, k = case["m"], case["n"], case["k"]
+    ldd = ldd or case["ldc"]
+    n_end = n if n_end is None else n_end
+    ref = orc.gemm_ref_f32(case["trans_a"], case["trans_b"], m, n, k, case["alpha"], case["A"], case["lda"],
+                           case["B"], case["ldb"], case["beta"], case["C"], case["ldc"], m, n_begin=n_begin,
+                           n_end=n_end, threads=threads)
+    G = mat(got_flat, m, n, ldd)[:, n_begin:n_end]
+    R = mat(ref, m, n, m)[:, n_begin:n_end]
+    opA = orc.op_matrix(case["A"], case["trans_a"], m, k, case["lda"])
+    opB = orc.op_matrix(case["B"], case["trans_b"], k, n, case["ldb"])[:, n_begin:n_end]
+    Cm = mat(case["C"], m, n, case["ldc"])[:, n_begin:n_end] if case["beta"] != 0 else None
+    assert_close(G, R, np.abs(opA) @ np.abs(opB), k, case["alpha"], case["beta"], Cm, case["out_dtype"], rounding)
+    return G, R

@@ -43,6 +43,8 @@ def test_struct_layout_matches_header():
     assert tl.Problem.alpha.offset == _c_sizeof("offsetof(tl_gemm_problem, alpha)")
     assert tl.Problem.out_rounding.offset == _c_sizeof("offsetof(tl_gemm_problem, out_rounding)")
     assert tl.Solution.ctas.offset == _c_sizeof("offsetof(tl_gemm_solution, ctas)")
+    assert tl.Solution.debug_flags.offset == _c_sizeof("offsetof(tl_gemm_solution, debug_flags)")
+    assert tl.DEBUG_SKIP_LOADS == _c_sizeof("TL_DEBUG_SKIP_LOADS")
 
 
 def test_tensile_kernarg_layout():

@@ -40,33 +40,9 @@ def fp32_tol(k):
     return 2e-6 * math.sqrt(max(k, 512) / 512.0)
 
 
-def ulp_out(x, od):
-    mag = np.maximum(np.abs(x), {"fp32": 2.0 ** -126, "fp16": 2.0 ** -14, "bf16": 2.0 ** -126}[od])
-    return 2.0 ** (np.floor(np.log2(mag)) - MANT[od])
-
-
-def assert_close(G, R, absprod, k, alpha, beta, Cm, od, rounding="rne"):
-    """G: GPU result (m x n, exact fp32 values of the output), R: oracle fp32 result.  Truncating
-    output rounding may lose a whole ulp instead of half of one."""
-    G = np.asarray(G, np.float64)
-    R = np.asarray(R, np.float64)
-    bound = ulp_out(R, od) + 3.0 * k * 2.0 ** -24 * abs(alpha) * absprod
-    if beta != 0.0 and Cm is not None:
-        bound = bound + 2.0 ** -23 * np.abs(beta * np.asarray(Cm, np.float64))
-    err = np.abs(G - R)
-    bad = int(np.count_nonzero(err > bound))
-    assert np.all(np.isfinite(G)), "non-finite output"
-    assert bad == 0, f"{bad} elements beyond the bound; worst excess {float(np.max(err - bound)):.3e}"
-    nw = orc.normwise_error(G, R)
-    allowance = 2.0 ** -(MANT[od] + (0 if rounding == "trunc" else 1)) + 3.0 * k * 2.0 ** -24 * abs(alpha) * float(np.max(absprod)) / max(
-        float(np.max(np.abs(R))), 1e-30)
-    assert nw <= allowance, f"normwise {nw:.3e} > {allowance:.3e}"
-
-
-def absprod_of(case):
-    opA = orc.op_matrix(case["A"], case["trans_a"], case["m"], case["k"], case["lda"])
-    opB = orc.op_matrix(case["B"], case["trans_b"], case["k"], case["n"], case["ldb"])
-    return np.abs(opA) @ np.abs(opB)
+ulp_out = gu.ulp_out
+assert_close = gu.assert_close
+absprod_of = gu.absprod_of
 
 
 def check_case(h, case, dt, kernel="auto", solution=None, rounding="rne"):
