@@ -659,6 +659,15 @@ def test_tensile_layout_launch_matches_gemm(h, dt, name):
     h.device_status()
     view = torch.int32 if dt == "fp32" else torch.int16
     assert torch.equal(D1.view(view), D2.view(view))
+    # and against the oracle's restated reference loop, batch by batch (bf16 stores truncate, as the
+    # reference's BBH kernel does)
+    rounding = "trunc" if dt == "bf16" else "rne"
+    Af, Bf, Cf = (gu.from_dev(x, dt) for x in (A, B, C))
+    got = gu.from_dev(D2, dt)
+    for b in range(batch):
+        case = dict(trans_a=True, trans_b=False, m=m, n=n, k=k, lda=lda, ldb=ldb, ldc=ldc, alpha=alpha, beta=beta,
+                    A=Af[b * sa:(b + 1) * sa], B=Bf[b * sb:(b + 1) * sb], C=Cf[b * sc:(b + 1) * sc], out_dtype=dt)
+        gu.check_against_oracle(got[b * sd:(b + 1) * sd], case, ldd=ldd, rounding=rounding)
     with pytest.raises(tl.TLError) as e:
         h.tensile_launch("Cijk_Ailk_Bljk_SB", buf)
     assert e.value.status == tl.ERR_UNSUPPORTED
@@ -694,6 +703,29 @@ def test_cli_runs_and_verifies(args):
     assert "Performance =" in out.stdout
     if "-t" not in args:
         assert "Verify Success" in out.stdout, out.stdout
+
+
+# ---------------------------------------------------------------------------- device data init
+@pytest.mark.parametrize("dt", ["fp32", "fp16", "bf16", "fp8"])
+def test_fill_pattern_matches_init_real_data(h, dt):
+    """tl_fill_pattern (device) against the oracle's InitRealData (ff_gpu_src/ff_gpu.cpp:110-148),
+    bit for bit: every flat-index code, converted to the buffer type with round-to-nearest-even
+    (saturating for fp8); the shape-dependent codes 2.2 / -2.2 are refused."""
+    import torch
+    count = 100003
+    nbytes = {"fp32": 4, "fp16": 2, "bf16": 2, "fp8": 1}[dt]
+    code_of = {"fp32": tl.FP32, "fp16": tl.FP16, "bf16": tl.BF16, "fp8": tl.FP8}[dt]
+    L = tl.lib()
+    buf = torch.empty(count * nbytes, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    for code in (0.0, 0.5, 1.0, 2.0, 2.1, 2.3, 2.4, -1.0, -2.0, -2.1, -2.3, -2.4, 3.25):
+        tl.check(L.tl_fill_pattern(code_of, buf.data_ptr(), count, code, stream))
+        torch.cuda.synchronize()
+        want = orc.encode(orc.init_pattern(code, count, 1), dt)
+        got = buf.cpu().numpy().view(want.dtype)
+        assert np.array_equal(got, want), f"code {code}: {int(np.count_nonzero(got != want))} elements differ"
+    for code in (2.2, -2.2):
+        assert L.tl_fill_pattern(code_of, buf.data_ptr(), count, code, stream) == tl.ERR_UNSUPPORTED
 
 
 # ---------------------------------------------------------------------------- fused epilogue
@@ -753,6 +785,15 @@ def test_fused_epilogue(h, dt, lay, act, cg, bm, split):
     bad = np.abs(got.astype(np.float64) - ref) > ulp + 1e-6 * np.abs(ref).max()
     assert int(bad.sum()) == 0, (got[bad][:5], ref[bad][:5])
     assert abs(amax.item() - np.abs(ref).max()) <= 1e-5 * np.abs(ref).max()
+    # against the oracle: the restated reference loop (alpha*AB + beta*C in fp32), then bias and the
+    # activation on the host; the activations are 1.13-Lipschitz at most, so the accumulation
+    # allowance carries over scaled by that
+    R0 = gu.mat(gu.oracle_ref(case), m, n, m)
+    Ro = _epi_ref(R0, bias, act).astype(np.float64)
+    acc = 3.0 * k * 2.0 ** -24 * 0.75 * gu.absprod_of(case) + 2.0 ** -23 * np.abs(0.5 * gu.mat(case["C"], m, n, m))
+    bound = 2.0 * ulp_out(Ro, dt) + 1.13 * acc + 1e-6 * np.abs(Ro).max()
+    bad = np.abs(got.astype(np.float64) - Ro) > bound
+    assert int(bad.sum()) == 0, (got[bad][:5], Ro[bad][:5])
 
 
 def test_fused_epilogue_errors_and_linear(h):
