@@ -217,10 +217,16 @@ typedef struct tl_epilogue {
     int32_t bias_dtype;   /* TL_DTYPE_FP32, FP16 or BF16 */
     int32_t activation;   /* tl_activation */
     float* amax;          /* NULL, or a device float */
-    int32_t reserved[4];
+    float d_scale;        /* fp8 (E4M3) output: D = e4m3(d_scale * act(...)), round to nearest even,
+                             saturating at +-448; 0 is read as 1; ignored for other outputs */
+    int32_t reserved[3];
 } tl_epilogue;
 
-/* tl_gemm with a fused epilogue (epilogue == NULL: tl_gemm). */
+/* tl_gemm with a fused epilogue (epilogue == NULL: tl_gemm).
+ * FP8 output (dtype_c = dtype_d = TL_DTYPE_FP8_E4M3, tensor-core kernels, beta == 0): the epilogue
+ * quantises D = e4m3(d_scale * act(alpha*op(A)*op(B) + bias)); amax, when set, receives the max |.|
+ * of the values before d_scale -- what the next step's scale is computed from.  tl_gemm with an fp8
+ * output is the same with no bias, no activation and d_scale 1. */
 TL_API tl_status tl_gemm_ex(tl_handle* handle, const tl_gemm_problem* problem, const tl_epilogue* epilogue,
                             const tl_gemm_solution* solution, void* D, const void* C, const void* A, const void* B,
                             void* stream);

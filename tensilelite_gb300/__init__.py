@@ -70,8 +70,8 @@ class Problem(ctypes.Structure):
         p = cls()
         dt = DTYPE_NAMES[dtype] if isinstance(dtype, str) else dtype
         od = dt if out_dtype is None else (DTYPE_NAMES[out_dtype] if isinstance(out_dtype, str) else out_dtype)
-        if od == FP8:
-            od = BF16
+        if od == FP8 and out_dtype is None:
+            od = BF16          # fp8 operands default to a bf16 output; ask for out_dtype="fp8" explicitly
         ta, tb = OP_T if trans_a else OP_N, OP_T if trans_b else OP_N
         check(lib().tl_problem_init(ctypes.byref(p), dt, od, ta, tb, m, n, k))
         p.batch = batch
@@ -100,7 +100,7 @@ ACTIVATIONS = {"none": 0, "relu": 1, "gelu": 2, "silu": 3}
 class Epilogue(ctypes.Structure):
     """tl_epilogue: D = act(alpha*op(A)*op(B) + beta*C + bias[row]); max |D| into *amax."""
     _fields_ = [("bias", ctypes.c_void_p), ("bias_dtype", ctypes.c_int32), ("activation", ctypes.c_int32),
-                ("amax", ctypes.c_void_p), ("reserved", ctypes.c_int32 * 4)]
+                ("amax", ctypes.c_void_p), ("d_scale", ctypes.c_float), ("reserved", ctypes.c_int32 * 3)]
 
 
 class Solution(ctypes.Structure):
@@ -319,9 +319,11 @@ class Handle:
         return n.value
 
     def gemm_ex(self, p: Problem, D, C, A, B, bias=None, bias_dtype=None, activation="none", amax=None,
-                solution: Optional[Solution] = None, stream=None):
-        """tl_gemm_ex: tl_gemm with a fused bias / activation / amax epilogue."""
+                d_scale=0.0, solution: Optional[Solution] = None, stream=None):
+        """tl_gemm_ex: tl_gemm with a fused bias / activation / amax epilogue (and, for an fp8 output,
+        the quantisation scale d_scale)."""
         e = Epilogue()
+        e.d_scale = d_scale
         e.bias = _ptr(bias)
         if bias is not None and bias_dtype is None:
             bias_dtype = torch_dtype_code(bias.dtype)

@@ -20,9 +20,11 @@ CLI = os.path.join(HERE, "tensilelite")
 
 SOURCES = ["gemm_tc.cu", "gemm_simt.cu", "aux_kernels.cu", "tl_api.cpp", "noalloc.cu"]
 # The tcgen05 kernel template is instantiated in generated units, one per operand kind (0 fp16/bf16,
-# 1 fp8), cluster size and epilogue variant (three output types each), so they compile in parallel.
-INSTANCES = [(k, e, cl) for k in (0, 1) for e in ((False, True) if k == 0 else (False,)) for cl in (1, 2, 4)]
+# 1 fp8), cluster size and epilogue variant, so they compile in parallel.  Plain kernels write fp32,
+# fp16 or bf16; the fused-epilogue kernels also fp8 (E4M3).
+INSTANCES = [(k, e, cl) for k in (0, 1) for e in (False, True) for cl in (1, 2, 4)]
 OUT_TYPES = ("float", "__half", "__nv_bfloat16")
+EPI_OUT_TYPES = OUT_TYPES + ("__nv_fp8_e4m3",)
 
 
 def _instance_sources():
@@ -31,7 +33,7 @@ def _instance_sources():
     paths = []
     for k, e, cl in INSTANCES:
         lines = ['#include "tensilelite_gb300/csrc/gemm_tc_kernel.cuh"', "namespace tl {", "namespace tc {"]
-        for td in OUT_TYPES:
+        for td in (EPI_OUT_TYPES if e else OUT_TYPES):
             lines.append(f"template tl_status launch_kernel<{k}, {td}, {cl}, {'true' if e else 'false'}>("
                          "const TcKernelParams&, int, size_t, cudaStream_t);")
             if not e:

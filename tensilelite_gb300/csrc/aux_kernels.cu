@@ -51,6 +51,9 @@ __device__ __forceinline__ void store_from_float(int dtype, int trunc, void* p, 
         if (trunc) static_cast<uint16_t*>(p)[i] = static_cast<uint16_t>(__float_as_uint(v) >> 16);
         else static_cast<__nv_bfloat16*>(p)[i] = __float2bfloat16_rn(v);
         break;
+    case TL_DTYPE_FP8_E4M3:
+        static_cast<uint8_t*>(p)[i] = static_cast<uint8_t>(__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3));
+        break;
     default: break;
     }
 }

@@ -2,12 +2,23 @@
 //
 // The plain-FP32 counterpart of TensileLite's sgemm path (the fp32 MFMA kernel,
 // src/gemmMfmaKernelWriter.h:38-40) and the generic fallback for operands the TMA path cannot
-// describe (leading dimensions that are not 16-byte multiples).  128x128 output tile per 256-thread
-// CTA, 8x8 outputs per thread in two 4-wide strips per dimension (or, when 128x128 tiles would leave
-// most SMs idle, 64x64 tiles with 4x4 outputs per thread), k staged 8 at a time through a
-// double-buffered shared-memory ring with the next slab prefetched into registers.  op(A)/op(B) of
-// either storage order are read with the thread mapping that keeps the contiguous dimension
-// coalesced; edge tiles are zero-filled on load and masked on store.
+// describe (leading dimensions that are not 16-byte multiples).
+//
+// Blackwell issues two fp32 FMAs per instruction (fma.rn.f32x2, __ffma2_rn): each thread keeps its
+// TM x TN accumulators as float2 pairs along m, and one packed FMA multiplies a pair of A values by
+// a B value held twice ({b, b}).  The B tile is therefore stored in shared memory with every value
+// duplicated, so the pairs come straight out of 16-byte shared loads with no packing instructions;
+// an outer-product step of 8 x 8 outputs is 2 + 4 shared loads and 32 packed FMAs.
+//
+// Two shapes (chosen per problem on the host):
+//   large  128 x 128 output tile, 256 threads, 8 x 8 outputs per thread, k in slabs of 8;
+//   small  64 x 32 output tile, 256 threads in 4 groups that each take a quarter of every k-slab
+//          (8 x 4 outputs per thread and group); the groups' partial tiles are summed in group order
+//          through shared memory at the end.  For problems whose 128 x 128 tiles would leave most SMs
+//          idle (the reference's 480 x 512 x 512 case: 16 large tiles, 128 small ones).
+// k-slabs are double-buffered in shared memory and prefetched into registers one slab ahead, with
+// 4-element vector loads along whichever dimension is contiguous in memory; edge tiles are
+// zero-filled on load and masked on store.  Results are deterministic (fixed summation order).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_fp8.h>
@@ -17,13 +28,32 @@
 namespace tl {
 namespace {
 
-constexpr int BK = 8, THREADS = 256;
-
 template <typename T> __device__ __forceinline__ float to_f(T v);
 template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
 template <> __device__ __forceinline__ float to_f<__half>(__half v) { return __half2float(v); }
 template <> __device__ __forceinline__ float to_f<__nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
 template <> __device__ __forceinline__ float to_f<__nv_fp8_e4m3>(__nv_fp8_e4m3 v) { return static_cast<float>(v); }
+
+// Four consecutive elements from a pointer aligned to 4 elements, widened to fp32.
+template <typename T> __device__ __forceinline__ float4 load4(const T* p);
+template <> __device__ __forceinline__ float4 load4<float>(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+template <> __device__ __forceinline__ float4 load4<__half>(const __half* p)
+{
+    const uint2 w = __ldg(reinterpret_cast<const uint2*>(p));
+    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&w.x));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&w.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+}
+template <> __device__ __forceinline__ float4 load4<__nv_bfloat16>(const __nv_bfloat16* p)
+{
+    const uint2 w = __ldg(reinterpret_cast<const uint2*>(p));
+    return make_float4(__uint_as_float(w.x << 16), __uint_as_float(w.x & 0xffff0000u), __uint_as_float(w.y << 16),
+                       __uint_as_float(w.y & 0xffff0000u));
+}
+template <> __device__ __forceinline__ float4 load4<__nv_fp8_e4m3>(const __nv_fp8_e4m3* p)
+{
+    return make_float4(to_f(p[0]), to_f(p[1]), to_f(p[2]), to_f(p[3]));
+}
 
 template <typename TD> __device__ __forceinline__ void store_out(TD* p, float v, int trunc);
 template <> __device__ __forceinline__ void store_out<float>(float* p, float v, int) { *p = v; }
@@ -45,66 +75,158 @@ struct SimtParams {
     int trans_a, trans_b;
     float alpha, beta;
     int out_trunc;
+    int vec_a, vec_b;      // 4-element vector loads are aligned along the contiguous dimension
 };
 
-// TM outputs per thread and dimension: 8 (128 x 128 tile) or 4 (64 x 64 tile), in TM/4 strips of 4
-template <typename TA, typename TD, int TM>
-__global__ void __launch_bounds__(THREADS, 2) simt_gemm_kernel(const SimtParams p)
+// Tile shape: BM x BN outputs, TM x TN per thread and k-group, KG k-groups, BKG k per group and slab.
+template <int BM_, int BN_, int TM_, int TN_, int KG_, int BKG_, int MINB_>
+struct Cfg {
+    static constexpr int BM = BM_, BN = BN_, TM = TM_, TN = TN_, KG = KG_, BKG = BKG_, MINB = MINB_;
+    static constexpr int TX = BM / TM;           // threads along m in a group
+    static constexpr int TY = BN / TN;           // threads along n
+    static constexpr int GT = TX * TY;           // threads per k-group
+    static constexpr int THREADS = GT * KG;
+    static constexpr int BK = BKG * KG;          // k per slab
+    static constexpr int SWM = TX * 4;           // width of one strip of 4 m-values per thread
+    static constexpr int SWN = TY * 4;
+    static constexpr int A_CHUNKS = BK * BM / 4 / THREADS;   // 4-element loads per thread and slab
+    static constexpr int B_CHUNKS = BK * BN / 4 / THREADS;
+    static constexpr int SMEM_FLOATS = 2 * BK * BM + 2 * BK * 2 * BN;
+    static constexpr int RED_FLOATS = KG > 1 ? KG * BM * BN : 0;
+    static constexpr size_t SMEM_BYTES = sizeof(float) * (SMEM_FLOATS > RED_FLOATS ? SMEM_FLOATS : RED_FLOATS);
+    static_assert(TM % 4 == 0 && TN % 4 == 0, "per-thread tiles are strips of 4");
+    static_assert(A_CHUNKS * THREADS * 4 == BK * BM && B_CHUNKS * THREADS * 4 == BK * BN, "whole slabs");
+};
+using CfgLarge = Cfg<128, 128, 8, 8, 1, 8, 2>;
+using CfgSmall = Cfg<64, 32, 8, 4, 4, 8, 2>;
+
+template <typename TA, typename TD, typename G>
+__global__ void __launch_bounds__(G::THREADS, G::MINB) simt_gemm_kernel(const SimtParams p)
 {
-    constexpr int BM = 16 * TM, BN = 16 * TM;   // 16 x 16 threads
-    constexpr int LOADS = BM * BK / THREADS;    // elements of A (and of B) each thread stages per slab
-    constexpr int STRIPS = TM / 4;
-    __shared__ __align__(16) float As[2][BK][BM];
-    __shared__ __align__(16) float Bs[2][BK][BN];
+    constexpr int BM = G::BM, BN = G::BN, BK = G::BK, TM = G::TM, TN = G::TN;
+    extern __shared__ __align__(16) float smem[];
+    float* As = smem;                        // [2][BK][BM]      op(A)(m, k) at [k][m]
+    float* Bs = smem + 2 * BK * BM;          // [2][BK][2 * BN]  op(B)(k, n) at [k][2n] and [k][2n + 1]
 
     const int tid = threadIdx.x;
-    const int tx = tid & 15;          // m strip
-    const int ty = tid >> 4;          // n strip
+    const int grp = tid / G::GT;             // k-group
+    const int gtid = tid % G::GT;
+    const int tx = gtid % G::TX;
+    const int ty = gtid / G::TX;
     const int m_blk = blockIdx.x * BM;
     const int n_blk = blockIdx.y * BN;
     const int b = blockIdx.z;
     const TA* A = static_cast<const TA*>(p.A) + static_cast<int64_t>(b) * p.sa;
     const TA* B = static_cast<const TA*>(p.B) + static_cast<int64_t>(b) * p.sb;
 
-    // per-thread load coordinates: LOADS elements of A and of B per k-slab
-    int a_m[LOADS], a_k[LOADS], b_n[LOADS], b_k[LOADS];
-#pragma unroll
-    for (int i = 0; i < LOADS; ++i) {
-        const int idx = tid + i * THREADS;
-        if (!p.trans_a) { a_m[i] = idx % BM; a_k[i] = idx / BM; }   // A[m + k*lda]: m contiguous
-        else { a_m[i] = idx / BK; a_k[i] = idx % BK; }              // A[k + m*lda]: k contiguous
-        if (p.trans_b) { b_n[i] = idx % BN; b_k[i] = idx / BN; }    // B[n + k*ldb]: n contiguous
-        else { b_n[i] = idx / BK; b_k[i] = idx % BK; }              // B[k + n*ldb]: k contiguous
-    }
-    float ra[LOADS], rb[LOADS];
+    // ---- global -> registers (one slab ahead) -> shared
+    float4 ra[G::A_CHUNKS], rb[G::B_CHUNKS];
     auto load_slab = [&](int k0) {
 #pragma unroll
-        for (int i = 0; i < LOADS; ++i) {
-            const int m = m_blk + a_m[i], k = k0 + a_k[i];
-            float v = 0.f;
-            if (m < p.M && k < p.K)
-                v = to_f<TA>(p.trans_a ? A[k + static_cast<int64_t>(m) * p.lda] : A[m + static_cast<int64_t>(k) * p.lda]);
-            ra[i] = v;
-            const int n = n_blk + b_n[i], kb = k0 + b_k[i];
-            float w = 0.f;
-            if (n < p.N && kb < p.K)
-                w = to_f<TA>(p.trans_b ? B[n + static_cast<int64_t>(kb) * p.ldb] : B[kb + static_cast<int64_t>(n) * p.ldb]);
-            rb[i] = w;
+        for (int c = 0; c < G::A_CHUNKS; ++c) {
+            const int idx = tid + c * G::THREADS;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (!p.trans_a) {                // A[m + k*lda]: 4 consecutive m of one k
+                const int m = m_blk + (idx % (BM / 4)) * 4, k = k0 + idx / (BM / 4);
+                const TA* src = A + m + static_cast<int64_t>(k) * p.lda;
+                if (k < p.K) {
+                    if (p.vec_a && m + 3 < p.M) v = load4<TA>(src);
+                    else {
+                        if (m < p.M) v.x = to_f<TA>(src[0]);
+                        if (m + 1 < p.M) v.y = to_f<TA>(src[1]);
+                        if (m + 2 < p.M) v.z = to_f<TA>(src[2]);
+                        if (m + 3 < p.M) v.w = to_f<TA>(src[3]);
+                    }
+                }
+            } else {                         // A[k + m*lda]: 4 consecutive k of one m
+                const int m = m_blk + idx % BM, k = k0 + (idx / BM) * 4;
+                const TA* src = A + k + static_cast<int64_t>(m) * p.lda;
+                if (m < p.M) {
+                    if (p.vec_a && k + 3 < p.K) v = load4<TA>(src);
+                    else {
+                        if (k < p.K) v.x = to_f<TA>(src[0]);
+                        if (k + 1 < p.K) v.y = to_f<TA>(src[1]);
+                        if (k + 2 < p.K) v.z = to_f<TA>(src[2]);
+                        if (k + 3 < p.K) v.w = to_f<TA>(src[3]);
+                    }
+                }
+            }
+            ra[c] = v;
+        }
+#pragma unroll
+        for (int c = 0; c < G::B_CHUNKS; ++c) {
+            const int idx = tid + c * G::THREADS;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (p.trans_b) {                 // B[n + k*ldb]: 4 consecutive n of one k
+                const int n = n_blk + (idx % (BN / 4)) * 4, k = k0 + idx / (BN / 4);
+                const TA* src = B + n + static_cast<int64_t>(k) * p.ldb;
+                if (k < p.K) {
+                    if (p.vec_b && n + 3 < p.N) v = load4<TA>(src);
+                    else {
+                        if (n < p.N) v.x = to_f<TA>(src[0]);
+                        if (n + 1 < p.N) v.y = to_f<TA>(src[1]);
+                        if (n + 2 < p.N) v.z = to_f<TA>(src[2]);
+                        if (n + 3 < p.N) v.w = to_f<TA>(src[3]);
+                    }
+                }
+            } else {                         // B[k + n*ldb]: 4 consecutive k of one n
+                const int n = n_blk + idx % BN, k = k0 + (idx / BN) * 4;
+                const TA* src = B + k + static_cast<int64_t>(n) * p.ldb;
+                if (n < p.N) {
+                    if (p.vec_b && k + 3 < p.K) v = load4<TA>(src);
+                    else {
+                        if (k < p.K) v.x = to_f<TA>(src[0]);
+                        if (k + 1 < p.K) v.y = to_f<TA>(src[1]);
+                        if (k + 2 < p.K) v.z = to_f<TA>(src[2]);
+                        if (k + 3 < p.K) v.w = to_f<TA>(src[3]);
+                    }
+                }
+            }
+            rb[c] = v;
         }
     };
     auto store_slab = [&](int buf) {
+        float* as = As + buf * BK * BM;
+        float* bs = Bs + buf * BK * 2 * BN;
 #pragma unroll
-        for (int i = 0; i < LOADS; ++i) {
-            As[buf][a_k[i]][a_m[i]] = ra[i];
-            Bs[buf][b_k[i]][b_n[i]] = rb[i];
+        for (int c = 0; c < G::A_CHUNKS; ++c) {
+            const int idx = tid + c * G::THREADS;
+            if (!p.trans_a) {
+                const int m = (idx % (BM / 4)) * 4, k = idx / (BM / 4);
+                *reinterpret_cast<float4*>(as + k * BM + m) = ra[c];
+            } else {
+                const int m = idx % BM, k = (idx / BM) * 4;
+                as[(k + 0) * BM + m] = ra[c].x;
+                as[(k + 1) * BM + m] = ra[c].y;
+                as[(k + 2) * BM + m] = ra[c].z;
+                as[(k + 3) * BM + m] = ra[c].w;
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < G::B_CHUNKS; ++c) {
+            const int idx = tid + c * G::THREADS;
+            if (p.trans_b) {
+                const int n = (idx % (BN / 4)) * 4, k = idx / (BN / 4);
+                float* row = bs + k * 2 * BN + 2 * n;
+                *reinterpret_cast<float4*>(row) = make_float4(rb[c].x, rb[c].x, rb[c].y, rb[c].y);
+                *reinterpret_cast<float4*>(row + 4) = make_float4(rb[c].z, rb[c].z, rb[c].w, rb[c].w);
+            } else {
+                const int n = idx % BN, k = (idx / BN) * 4;
+                *reinterpret_cast<float2*>(bs + (k + 0) * 2 * BN + 2 * n) = make_float2(rb[c].x, rb[c].x);
+                *reinterpret_cast<float2*>(bs + (k + 1) * 2 * BN + 2 * n) = make_float2(rb[c].y, rb[c].y);
+                *reinterpret_cast<float2*>(bs + (k + 2) * 2 * BN + 2 * n) = make_float2(rb[c].z, rb[c].z);
+                *reinterpret_cast<float2*>(bs + (k + 3) * 2 * BN + 2 * n) = make_float2(rb[c].w, rb[c].w);
+            }
         }
     };
 
-    float acc[TM][TM];
+    // acc[i][j] holds outputs (m_{2i}, n_j) and (m_{2i+1}, n_j); m_r = (r/4)*SWM + tx*4 + r%4,
+    // n_j = (j/4)*SWN + ty*4 + j%4
+    float2 acc[TM / 2][TN];
 #pragma unroll
-    for (int i = 0; i < TM; ++i)
+    for (int i = 0; i < TM / 2; ++i)
 #pragma unroll
-        for (int j = 0; j < TM; ++j) acc[i][j] = 0.f;
+        for (int j = 0; j < TN; ++j) acc[i][j] = make_float2(0.f, 0.f);
 
     const int nslab = (p.K + BK - 1) / BK;
     if (nslab > 0) {
@@ -115,42 +237,90 @@ __global__ void __launch_bounds__(THREADS, 2) simt_gemm_kernel(const SimtParams 
     for (int s = 0; s < nslab; ++s) {
         const int buf = s & 1;
         if (s + 1 < nslab) load_slab((s + 1) * BK);
+        const float* as = As + buf * BK * BM + grp * G::BKG * BM;
+        const float* bs = Bs + buf * BK * 2 * BN + grp * G::BKG * 2 * BN;
 #pragma unroll
-        for (int k = 0; k < BK; ++k) {
-            float a[TM], bb[TM];
+        for (int kk = 0; kk < G::BKG; ++kk) {
+            float2 a[TM / 2], bd[TN];
 #pragma unroll
-            for (int st = 0; st < STRIPS; ++st) {
-                const float4 av = *reinterpret_cast<const float4*>(&As[buf][k][st * 64 + tx * 4]);
-                const float4 bv = *reinterpret_cast<const float4*>(&Bs[buf][k][st * 64 + ty * 4]);
-                a[4 * st] = av.x; a[4 * st + 1] = av.y; a[4 * st + 2] = av.z; a[4 * st + 3] = av.w;
-                bb[4 * st] = bv.x; bb[4 * st + 1] = bv.y; bb[4 * st + 2] = bv.z; bb[4 * st + 3] = bv.w;
+            for (int st = 0; st < TM / 4; ++st) {
+                const float4 v = *reinterpret_cast<const float4*>(as + kk * BM + st * G::SWM + tx * 4);
+                a[2 * st] = make_float2(v.x, v.y);
+                a[2 * st + 1] = make_float2(v.z, v.w);
             }
 #pragma unroll
-            for (int i = 0; i < TM; ++i)
+            for (int st = 0; st < TN / 4; ++st) {
+                const float* row = bs + kk * 2 * BN + 2 * (st * G::SWN + ty * 4);
+                const float4 v0 = *reinterpret_cast<const float4*>(row);
+                const float4 v1 = *reinterpret_cast<const float4*>(row + 4);
+                bd[4 * st + 0] = make_float2(v0.x, v0.y);
+                bd[4 * st + 1] = make_float2(v0.z, v0.w);
+                bd[4 * st + 2] = make_float2(v1.x, v1.y);
+                bd[4 * st + 3] = make_float2(v1.z, v1.w);
+            }
 #pragma unroll
-                for (int j = 0; j < TM; ++j) acc[i][j] = fmaf(a[i], bb[j], acc[i][j]);
+            for (int i = 0; i < TM / 2; ++i)
+#pragma unroll
+                for (int j = 0; j < TN; ++j) acc[i][j] = __ffma2_rn(a[i], bd[j], acc[i][j]);
         }
         if (s + 1 < nslab) store_slab(buf ^ 1);
         __syncthreads();
     }
 
-    // epilogue: D = alpha*acc + beta*C (C not read when beta == 0)
+    // ---- epilogue: D = alpha*acc + beta*C (C not read when beta == 0)
     TD* D = static_cast<TD*>(p.D) + static_cast<int64_t>(b) * p.sd;
     const TD* C = p.C ? static_cast<const TD*>(p.C) + static_cast<int64_t>(b) * p.sc : nullptr;
     const bool use_c = (p.beta != 0.f) && (C != nullptr);
+    auto finish = [&](int m, int n, float v) {
+        float o = p.alpha * v;
+        if (use_c) o = fmaf(p.alpha, v, p.beta * load_out<TD>(C + m + static_cast<int64_t>(n) * p.ldc));
+        store_out<TD>(D + m + static_cast<int64_t>(n) * p.ldd, o, p.out_trunc);
+    };
+    if constexpr (G::KG == 1) {
 #pragma unroll
-    for (int j = 0; j < TM; ++j) {
-        const int n = n_blk + (j / 4) * 64 + ty * 4 + (j % 4);
-        if (n >= p.N) continue;
+        for (int j = 0; j < TN; ++j) {
+            const int n = n_blk + (j / 4) * G::SWN + ty * 4 + (j % 4);
+            if (n >= p.N) continue;
 #pragma unroll
-        for (int i = 0; i < TM; ++i) {
-            const int m = m_blk + (i / 4) * 64 + tx * 4 + (i % 4);
-            if (m >= p.M) continue;
-            float v = p.alpha * acc[i][j];
-            if (use_c) v = fmaf(p.alpha, acc[i][j], p.beta * load_out<TD>(C + m + static_cast<int64_t>(n) * p.ldc));
-            store_out<TD>(D + m + static_cast<int64_t>(n) * p.ldd, v, p.out_trunc);
+            for (int i = 0; i < TM / 2; ++i) {
+                const int m = m_blk + ((2 * i) / 4) * G::SWM + tx * 4 + (2 * i) % 4;
+                if (m < p.M) finish(m, n, acc[i][j].x);
+                if (m + 1 < p.M) finish(m + 1, n, acc[i][j].y);
+            }
+        }
+    } else {
+        // the k-groups' partial tiles, [group][n][m], summed in group order
+        float* red = smem;                   // the slab buffers are free after the last sync
+#pragma unroll
+        for (int j = 0; j < TN; ++j) {
+            const int n = (j / 4) * G::SWN + ty * 4 + (j % 4);
+#pragma unroll
+            for (int i = 0; i < TM / 2; ++i) {
+                const int m = ((2 * i) / 4) * G::SWM + tx * 4 + (2 * i) % 4;
+                *reinterpret_cast<float2*>(red + (grp * BN + n) * BM + m) = acc[i][j];
+            }
+        }
+        __syncthreads();
+        for (int e = tid; e < BM * BN; e += G::THREADS) {
+            const int m = e % BM, n = e / BM;
+            float v = red[n * BM + m];
+#pragma unroll
+            for (int g = 1; g < G::KG; ++g) v += red[(g * BN + n) * BM + m];
+            if (m_blk + m < p.M && n_blk + n < p.N) finish(m_blk + m, n_blk + n, v);
         }
     }
+}
+
+template <typename TA, typename TD, typename G>
+tl_status launch_cfg(const SimtParams& p, int64_t M, int64_t N, int64_t batch, cudaStream_t s)
+{
+    auto kern = simt_gemm_kernel<TA, TD, G>;
+    dim3 grid(static_cast<unsigned>((M + G::BM - 1) / G::BM), static_cast<unsigned>((N + G::BN - 1) / G::BN),
+              static_cast<unsigned>(batch));
+    kern<<<grid, G::THREADS, G::SMEM_BYTES, s>>>(p);          // <= 48 KB: no opt-in needed
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "simt_gemm_kernel launch");
+    return TL_SUCCESS;
 }
 
 template <typename TA, typename TD>
@@ -164,26 +334,20 @@ tl_status launch(const SimtLaunch& L, cudaStream_t s)
     p.trans_a = L.trans_a; p.trans_b = L.trans_b;
     p.alpha = L.alpha; p.beta = L.beta;
     p.out_trunc = L.out_trunc;
-    // 128 x 128 tiles, or 64 x 64 when the larger tiles would occupy fewer than half of the SMs
+    // vector loads need the 4-element groups aligned: base, leading dimension and batch stride
+    const uintptr_t vb = 4 * sizeof(TA);
+    p.vec_a = ((reinterpret_cast<uintptr_t>(L.A) % vb) == 0 && L.lda % 4 == 0 && (L.batch == 1 || L.sa % 4 == 0)) ? 1 : 0;
+    p.vec_b = ((reinterpret_cast<uintptr_t>(L.B) % vb) == 0 && L.ldb % 4 == 0 && (L.batch == 1 || L.sb % 4 == 0)) ? 1 : 0;
     static const int sms = [] {
         int dev = 0, n = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
         return n > 0 ? n : 1;
     }();
+    // 128 x 128 tiles, or the k-grouped 64 x 32 tiles when the large ones would leave SMs idle
     const int64_t big_tiles = ((L.M + 127) / 128) * ((L.N + 127) / 128) * L.batch;
-    if (2 * big_tiles < sms) {
-        dim3 grid(static_cast<unsigned>((L.M + 63) / 64), static_cast<unsigned>((L.N + 63) / 64),
-                  static_cast<unsigned>(L.batch));
-        simt_gemm_kernel<TA, TD, 4><<<grid, THREADS, 0, s>>>(p);
-    } else {
-        dim3 grid(static_cast<unsigned>((L.M + 127) / 128), static_cast<unsigned>((L.N + 127) / 128),
-                  static_cast<unsigned>(L.batch));
-        simt_gemm_kernel<TA, TD, 8><<<grid, THREADS, 0, s>>>(p);
-    }
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "simt_gemm_kernel launch");
-    return TL_SUCCESS;
+    if (big_tiles < sms) return launch_cfg<TA, TD, CfgSmall>(p, L.M, L.N, L.batch, s);
+    return launch_cfg<TA, TD, CfgLarge>(p, L.M, L.N, L.batch, s);
 }
 
 template <typename TA>
@@ -203,7 +367,7 @@ tl_status simt_gemm_launch(const SimtLaunch& L, cudaStream_t s, int64_t* launche
 {
     if (L.M > 0x7fffffff || L.N > 0x7fffffff || L.K > 0x7fffffff || L.batch > 65535)
         return fail(TL_ERR_UNSUPPORTED, "SIMT kernel: dimension too large");
-    if ((L.N + 63) / 64 > 65535) return fail(TL_ERR_UNSUPPORTED, "SIMT kernel: n too large");
+    if ((L.N + 31) / 32 > 65535) return fail(TL_ERR_UNSUPPORTED, "SIMT kernel: n too large");
     tl_status st;
     switch (L.a_dtype) {
     case TL_DTYPE_FP32: st = launch_out<float>(L, s); break;

@@ -35,51 +35,22 @@ namespace tl {
 namespace tc {
 
 // instantiated in the generated instance units (one per operand kind, cluster size, epilogue)
-extern template tl_status launch_kernel<0, float, 1, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, __half, 1, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, __nv_bfloat16, 1, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, float, 2, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, __half, 2, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, __nv_bfloat16, 2, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, float, 4, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, __half, 4, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, __nv_bfloat16, 4, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, float, 1, true>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, __half, 1, true>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, __nv_bfloat16, 1, true>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, float, 2, true>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, __half, 2, true>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, __nv_bfloat16, 2, true>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, float, 4, true>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, __half, 4, true>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<0, __nv_bfloat16, 4, true>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<1, float, 1, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<1, __half, 1, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<1, __nv_bfloat16, 1, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<1, float, 2, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<1, __half, 2, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<1, __nv_bfloat16, 2, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<1, float, 4, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<1, __half, 4, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template tl_status launch_kernel<1, __nv_bfloat16, 4, false>(const TcKernelParams&, int, size_t, cudaStream_t);
-extern template int max_clusters<0, float, 1>(size_t);
-extern template int max_clusters<0, __half, 1>(size_t);
-extern template int max_clusters<0, __nv_bfloat16, 1>(size_t);
-extern template int max_clusters<0, float, 2>(size_t);
-extern template int max_clusters<0, __half, 2>(size_t);
-extern template int max_clusters<0, __nv_bfloat16, 2>(size_t);
-extern template int max_clusters<0, float, 4>(size_t);
-extern template int max_clusters<0, __half, 4>(size_t);
-extern template int max_clusters<0, __nv_bfloat16, 4>(size_t);
-extern template int max_clusters<1, float, 1>(size_t);
-extern template int max_clusters<1, __half, 1>(size_t);
-extern template int max_clusters<1, __nv_bfloat16, 1>(size_t);
-extern template int max_clusters<1, float, 2>(size_t);
-extern template int max_clusters<1, __half, 2>(size_t);
-extern template int max_clusters<1, __nv_bfloat16, 2>(size_t);
-extern template int max_clusters<1, float, 4>(size_t);
-extern template int max_clusters<1, __half, 4>(size_t);
-extern template int max_clusters<1, __nv_bfloat16, 4>(size_t);
+#define TL_TC_EXTERN(K, TD, CL, E) extern template tl_status launch_kernel<K, TD, CL, E>(const TcKernelParams&, int, size_t, cudaStream_t);
+#define TL_TC_EXTERN_CL(K, CL)                                                                                 \
+    TL_TC_EXTERN(K, float, CL, false) TL_TC_EXTERN(K, __half, CL, false) TL_TC_EXTERN(K, __nv_bfloat16, CL, false) \
+    TL_TC_EXTERN(K, float, CL, true) TL_TC_EXTERN(K, __half, CL, true) TL_TC_EXTERN(K, __nv_bfloat16, CL, true)    \
+    TL_TC_EXTERN(K, __nv_fp8_e4m3, CL, true)                                                                  \
+    extern template int max_clusters<K, float, CL>(size_t);                                                   \
+    extern template int max_clusters<K, __half, CL>(size_t);                                                  \
+    extern template int max_clusters<K, __nv_bfloat16, CL>(size_t);
+TL_TC_EXTERN_CL(0, 1)
+TL_TC_EXTERN_CL(0, 2)
+TL_TC_EXTERN_CL(0, 4)
+TL_TC_EXTERN_CL(1, 1)
+TL_TC_EXTERN_CL(1, 2)
+TL_TC_EXTERN_CL(1, 4)
+#undef TL_TC_EXTERN_CL
+#undef TL_TC_EXTERN
 
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -145,11 +116,18 @@ tl_status dispatch_cl(int in_dtype, int out_dtype, const TcKernelParams& kp, int
 {
     const int kind = (in_dtype == TL_DTYPE_FP8_E4M3) ? 1 : 0;
     if (kp.epi_on) {
-        // the fused-epilogue kernels: fp16/bf16 operands
-        if (kind != 0) return fail(TL_ERR_UNSUPPORTED, "a fused epilogue needs fp16/bf16 operands");
-        if (out_dtype == TL_DTYPE_FP32) return launch_kernel<0, float, CL, true>(kp, grid, smem, s);
-        if (out_dtype == TL_DTYPE_FP16) return launch_kernel<0, __half, CL, true>(kp, grid, smem, s);
-        if (out_dtype == TL_DTYPE_BF16) return launch_kernel<0, __nv_bfloat16, CL, true>(kp, grid, smem, s);
+        // the fused-epilogue kernels (they also write every fp8 output)
+        if (kind == 0) {
+            if (out_dtype == TL_DTYPE_FP32) return launch_kernel<0, float, CL, true>(kp, grid, smem, s);
+            if (out_dtype == TL_DTYPE_FP16) return launch_kernel<0, __half, CL, true>(kp, grid, smem, s);
+            if (out_dtype == TL_DTYPE_BF16) return launch_kernel<0, __nv_bfloat16, CL, true>(kp, grid, smem, s);
+            if (out_dtype == TL_DTYPE_FP8_E4M3) return launch_kernel<0, __nv_fp8_e4m3, CL, true>(kp, grid, smem, s);
+        } else {
+            if (out_dtype == TL_DTYPE_FP32) return launch_kernel<1, float, CL, true>(kp, grid, smem, s);
+            if (out_dtype == TL_DTYPE_FP16) return launch_kernel<1, __half, CL, true>(kp, grid, smem, s);
+            if (out_dtype == TL_DTYPE_BF16) return launch_kernel<1, __nv_bfloat16, CL, true>(kp, grid, smem, s);
+            if (out_dtype == TL_DTYPE_FP8_E4M3) return launch_kernel<1, __nv_fp8_e4m3, CL, true>(kp, grid, smem, s);
+        }
         return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel: unsupported output type");
     }
     if (kind == 0) {
@@ -300,7 +278,8 @@ bool tc_encode_output(CUtensorMap* tm, int out_dtype, void* D, int64_t M, int64_
     if ((reinterpret_cast<uintptr_t>(D) & 15) || (ldd * es) % 16 || (batch > 1 && (stride_d * es) % 16)) return false;
     const CUtensorMapDataType dt = out_dtype == TL_DTYPE_FP32   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
                                    : out_dtype == TL_DTYPE_FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
-                                                                : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+                                   : out_dtype == TL_DTYPE_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                                                : CU_TENSOR_MAP_DATA_TYPE_UINT8;
     cuuint64_t dims[3] = {static_cast<cuuint64_t>(M), static_cast<cuuint64_t>(N), static_cast<cuuint64_t>(batch)};
     cuuint64_t strides[2] = {static_cast<cuuint64_t>(ldd) * es,
                              batch > 1 ? static_cast<cuuint64_t>(stride_d) * es
@@ -430,6 +409,7 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     desc_params(L.in_dtype, kp.m_mn_major, kp.m_lbo, kp.m_kstep);
     kp.out_trunc = L.out_trunc;
     kp.epi_on = L.epi_on;
+    kp.epi_dscale = L.epi_dscale;
     kp.epi_bias = L.epi_bias;
     kp.epi_amax = L.epi_amax;
     kp.epi_bias_dtype = L.epi_bias_dtype;
@@ -440,7 +420,8 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
         kp.par_reduce = (kp.split_units > 0 && kp.bal_kb == 0 && kp.split_units <= workers && par_reduce_enabled()) ? 1 : 0;
     }
     // whole tiles leave through TMA stores (not with promotion, which drains chains into registers)
-    kp.tma_store = (L.promote_k == 0 && tma_store_enabled() &&
+    // (an fp8 output's 128-byte box is 128 columns wide: only tiles made of whole boxes)
+    kp.tma_store = (L.promote_k == 0 && tma_store_enabled() && (L.out_dtype != TL_DTYPE_FP8_E4M3 || L.bm % 128 == 0) &&
                     tc_encode_output(&kp.tmD, L.out_dtype, L.D, L.M, L.N, L.ldd, L.batch, L.stride_d))
                        ? 1
                        : 0;

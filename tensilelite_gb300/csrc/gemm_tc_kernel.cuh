@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <cuda_fp8.h>
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -27,6 +28,7 @@ struct TcKernelParams {
     // max |D| into *epi_amax
     const void* epi_bias;
     float* epi_amax;
+    float epi_dscale;             // fp8 outputs: values are multiplied by this before the E4M3 rounding
     int epi_bias_dtype;
     int epi_act;
     int epi_on;
@@ -235,6 +237,33 @@ template <> struct Out<__nv_bfloat16> {
     static constexpr int kBytes = 2;
 };
 
+// E4M3 outputs (fused-epilogue kernels; beta must be 0): round to nearest even, saturating to +-448.
+template <> struct Out<__nv_fp8_e4m3> {
+    __device__ static __forceinline__ float load(const void* base, int64_t idx)
+    {
+        return __half2float(__half(__nv_cvt_fp8_to_halfraw(static_cast<const __nv_fp8_storage_t*>(base)[idx], __NV_E4M3)));
+    }
+    __device__ static __forceinline__ void store(void* base, int64_t idx, float v, int)
+    { static_cast<__nv_fp8_storage_t*>(base)[idx] = __nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3); }
+    static constexpr int kBytes = 1;
+};
+
+// Four values as four E4M3 bytes in one word (first value in the low byte).
+__device__ __forceinline__ uint32_t pack4_e4m3(float a, float b, float c, float d)
+{
+    const uint32_t lo = __nv_cvt_float2_to_fp8x2(make_float2(a, b), __NV_SATFINITE, __NV_E4M3);
+    const uint32_t hi = __nv_cvt_float2_to_fp8x2(make_float2(c, d), __NV_SATFINITE, __NV_E4M3);
+    return (lo & 0xffffu) | (hi << 16);
+}
+
+// The quantisation scale of fp8 outputs (applied after the epilogue function and the amax).
+template <typename TD>
+__device__ __forceinline__ float out_scale(const TcKernelParams& p, float o)
+{
+    if constexpr (sizeof(TD) == 1) return o * p.epi_dscale;
+    else return o;
+}
+
 __device__ __forceinline__ uint32_t pack2(float a, float b, int is_half, int trunc)
 {
     if (is_half) {
@@ -318,6 +347,22 @@ __device__ __forceinline__ void store_chunk(const TcKernelParams& p, float& amax
                 }
                 reinterpret_cast<float4*>(dptr)[q] = o;
             }
+        } else if constexpr (sizeof(TD) == 1) {
+            // E4M3: 32 outputs in two 16-byte stores (no C: fp8 outputs take beta == 0)
+            uint32_t ow[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                float o[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    o[t] = j.alpha * acc[4 * q + t];
+                    if constexpr (EPI) o[t] = epi_fn(p, m + 4 * q + t, true, o[t], amax);
+                    o[t] = out_scale<TD>(p, o[t]);
+                }
+                ow[q] = pack4_e4m3(o[0], o[1], o[2], o[3]);
+            }
+            reinterpret_cast<uint4*>(dptr)[0] = make_uint4(ow[0], ow[1], ow[2], ow[3]);
+            reinterpret_cast<uint4*>(dptr)[1] = make_uint4(ow[4], ow[5], ow[6], ow[7]);
         } else {
             constexpr int is_half = std::is_same<TD, __half>::value ? 1 : 0;
 #pragma unroll
@@ -350,7 +395,7 @@ __device__ __forceinline__ void store_chunk(const TcKernelParams& p, float& amax
                 if (use_c) o = fmaf(j.alpha, acc[i], j.beta * Out<TD>::load(j.C, base_c + m + i));
                 else o = j.alpha * acc[i];
                 if constexpr (EPI) o = epi_fn(p, m + i, true, o, amax);
-                Out<TD>::store(j.D, base_d + m + i, o, trunc);
+                Out<TD>::store(j.D, base_d + m + i, out_scale<TD>(p, o), trunc);
             }
         }
     }
@@ -414,6 +459,7 @@ __device__ __forceinline__ void split_finish(const TcKernelParams& p, float& ama
 template <typename TD>
 __device__ __forceinline__ void load_c_chunk(const TileJob& j, int64_t base_c, int m, uint32_t (&cw)[32])
 {
+    if constexpr (sizeof(TD) == 1) return;        // fp8 outputs take beta == 0: no C
     if (!(j.beta != 0.0f && j.C != nullptr) || m >= j.M) return;
     const char* cptr = static_cast<const char*>(j.C) + (base_c + m) * Out<TD>::kBytes;
     if (m + 32 <= j.M && (reinterpret_cast<uintptr_t>(cptr) & 15) == 0) {
@@ -459,6 +505,19 @@ __device__ __forceinline__ void finish_pack(const TcKernelParams& p, float& amax
             float o = use_c ? fmaf(j.alpha, a, j.beta * __uint_as_float(cw[i])) : j.alpha * a;
             if constexpr (EPI) o = epi_fn(p, m + i, row_ok && m + i < j.M, o, amax);
             out[i] = __float_as_uint(o);
+        }
+    } else if constexpr (sizeof(TD) == 1) {
+        // E4M3: 32 outputs in 8 words (no C: fp8 outputs take beta == 0)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            float o[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                o[t] = j.alpha * __uint_as_float(r[4 * q + t]);
+                if constexpr (EPI) o[t] = epi_fn(p, m + 4 * q + t, row_ok && m + 4 * q + t < j.M, o[t], amax);
+                o[t] = out_scale<TD>(p, o[t]);
+            }
+            out[q] = pack4_e4m3(o[0], o[1], o[2], o[3]);
         }
     } else {
         constexpr int is_half = std::is_same<TD, __half>::value ? 1 : 0;
@@ -564,7 +623,7 @@ __device__ __forceinline__ void split_finish_tmem(const TcKernelParams& p, float
         // CPS 32-column chunks per step (two for 16-bit outputs, one for fp32, whose C takes twice
         // the registers): their C values and every other split's partials are in flight together
         // (the reduction is latency-bound), summed in split order
-        constexpr int CPS = sizeof(TD) == 4 ? 1 : 2;
+        constexpr int CPS = sizeof(TD) == 2 ? 2 : 1;
         const int chunks = p.bm / 32;     // even: bm is 64, 128, 192 or 256
         const size_t slab_elems = static_cast<size_t>(kTcTileN) * p.bm;
         const float* base = p.ws + static_cast<size_t>(j.slot) * p.tail_split * slab_elems + row;

@@ -120,7 +120,11 @@ tl_status validate(const tl_gemm_problem* p)
         return fail(TL_ERR_INVALID_ARG, "unknown dtype");
     if (p->dtype_a != p->dtype_b) return fail(TL_ERR_UNSUPPORTED, "dtype_a != dtype_b");
     if (p->dtype_c != p->dtype_d) return fail(TL_ERR_UNSUPPORTED, "dtype_c != dtype_d");
-    if (p->dtype_d == TL_DTYPE_FP8_E4M3) return fail(TL_ERR_UNSUPPORTED, "fp8 output is not supported");
+    if (p->dtype_d == TL_DTYPE_FP8_E4M3) {
+        // E4M3 outputs come out of the tensor-core epilogue, with no C operand
+        if (p->beta != 0.0f) return fail(TL_ERR_UNSUPPORTED, "an fp8 output takes beta == 0 (no fp8 C operand)");
+        if (p->kernel == TL_KERNEL_SIMT) return fail(TL_ERR_UNSUPPORTED, "the CUDA-core kernel writes no fp8 output");
+    }
     if (p->dtype_a == TL_DTYPE_FP32 && p->dtype_d != TL_DTYPE_FP32)
         return fail(TL_ERR_UNSUPPORTED, "fp32 inputs need an fp32 output");
     if ((p->trans_a != TL_OP_N && p->trans_a != TL_OP_T) || (p->trans_b != TL_OP_N && p->trans_b != TL_OP_T))
@@ -559,7 +563,7 @@ tl_status prepare(tl_handle* h, const tl_gemm_problem* prob, const tl_gemm_solut
     std::string why;
     const bool has_work = p.m > 0 && p.n > 0 && p.k > 0;
     if (kernel == TL_KERNEL_TCGEN05 && has_work && !tma_ok(p, A, B, &why)) {
-        if (p.kernel == TL_KERNEL_AUTO && !sol) {
+        if (p.kernel == TL_KERNEL_AUTO && !sol && p.dtype_d != TL_DTYPE_FP8_E4M3) {
             kernel = TL_KERNEL_SIMT;
             simt_solution(&P.s);
         } else {
@@ -744,7 +748,9 @@ tl_status enqueue(tl_handle* h, const Prepared& P, cudaStream_t s)
     L.counters_len = h->counters_len;
     L.tail_split = P.s.tail_split;
     L.sm_count = h->sm_count;
-    L.epi_on = P.epi_on ? 1 : 0;
+    // fp8 outputs are written by the fused-epilogue kernels (no bias or activation unless asked for)
+    L.epi_on = (P.epi_on || p.dtype_d == TL_DTYPE_FP8_E4M3) ? 1 : 0;
+    L.epi_dscale = (P.epi_on && P.epi.d_scale != 0.0f) ? P.epi.d_scale : 1.0f;
     L.epi_bias = P.epi.bias;
     L.epi_amax = P.epi.amax;
     L.epi_bias_dtype = P.epi.bias_dtype;
@@ -891,6 +897,8 @@ tl_status plan_tc_noalloc(int device, int sm_count, size_t smem_optin, const tl_
     L->cg = cgp;
     L->tail_split = 1;     // the static scratch is sized for explicit split-k only
     L->debug_flags = s.debug_flags;
+    L->epi_on = p.dtype_d == TL_DTYPE_FP8_E4M3 ? 1 : 0;     // fp8 outputs come out of the epilogue kernels
+    L->epi_dscale = 1.0f;
     L->sm_count = sm_count;
     return TL_SUCCESS;
 }
@@ -1189,6 +1197,8 @@ TL_API tl_status tl_gemm_ex(tl_handle* h, const tl_gemm_problem* p, const tl_epi
         return fail(TL_ERR_INVALID_ARG, "epilogue bias is not aligned to its element size");
     if (epi->amax && (reinterpret_cast<uintptr_t>(epi->amax) & 3))
         return fail(TL_ERR_INVALID_ARG, "epilogue amax is not 4-byte aligned");
+    if (!(epi->d_scale >= 0.0f) || std::isinf(epi->d_scale))
+        return fail(TL_ERR_INVALID_ARG, "epilogue d_scale must be finite and >= 0 (0 is read as 1)");
     Prepared P;
     t_capturing = stream_capturing(S(stream));
     if (t_capturing) h->captured = true;
@@ -1201,7 +1211,8 @@ TL_API tl_status tl_gemm_ex(tl_handle* h, const tl_gemm_problem* p, const tl_epi
     if (P.p.k == 0 || P.p.m == 0 || P.p.n == 0)
         return fail(TL_ERR_UNSUPPORTED, "a fused epilogue needs m, n, k > 0");
     P.epi = *epi;
-    P.epi_on = epi->bias != nullptr || epi->activation != TL_ACT_NONE || epi->amax != nullptr;
+    P.epi_on = epi->bias != nullptr || epi->activation != TL_ACT_NONE || epi->amax != nullptr ||
+               (P.p.dtype_d == TL_DTYPE_FP8_E4M3 && epi->d_scale != 0.0f && epi->d_scale != 1.0f);
     return enqueue(h, P, S(stream));
 }
 
@@ -1357,6 +1368,7 @@ TL_API tl_status tl_grouped_plan_create(tl_handle* h, const tl_gemm_problem* pro
             p.out_rounding != p0.out_rounding)
             return fail(TL_ERR_UNSUPPORTED, "grouped problems must share dtypes, trans flags and rounding");
         if (p.batch != 1) return fail(TL_ERR_UNSUPPORTED, "grouped problems must have batch == 1");
+        if (p.dtype_d == TL_DTYPE_FP8_E4M3) return fail(TL_ERR_UNSUPPORTED, "grouped GEMM writes no fp8 output");
         if (p.k == 0) return fail(TL_ERR_UNSUPPORTED, "grouped problems need k > 0");
         if (p.beta != 0.0f && (!C || !C[i])) return fail(TL_ERR_INVALID_ARG, "C missing with beta != 0");
         std::string why;

@@ -96,6 +96,7 @@ struct TcLaunch {
     // fused epilogue: D = act(alpha*acc + beta*C + bias[m]); max |D| into *epi_amax
     const void* epi_bias;
     float* epi_amax;
+    float epi_dscale;        // fp8 outputs: multiplied in before the E4M3 rounding
     int epi_bias_dtype;
     int epi_act;
     int epi_on;

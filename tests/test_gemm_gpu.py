@@ -796,6 +796,66 @@ def test_fused_epilogue(h, dt, lay, act, cg, bm, split):
     assert int(bad.sum()) == 0, (got[bad][:5], Ro[bad][:5])
 
 
+@pytest.mark.parametrize("dt,lay,act,cg,bm,split", [
+    ("bf16", "NN", "none", 1, 128, 1), ("bf16", "TN", "gelu", 2, 256, 1), ("fp16", "NT", "relu", 1, 64, 1),
+    ("fp8", "TN", "silu", 1, 256, 1), ("bf16", "NN", "relu", 1, 128, 3), ("fp8", "TN", "none", 2, 128, 2)])
+def test_fp8_output_epilogue(h, dt, lay, act, cg, bm, split):
+    """E4M3 output from the fused epilogue: D = e4m3(d_scale * act(alpha*AB + bias)), round to nearest
+    even, saturating.  Checked against the oracle's loop with the epilogue applied on the host and the
+    oracle's E4M3 quantiser (orc_f32_to_e4m3): every element within one E4M3 step of the quantised
+    oracle value, and nearly all bit-equal; the amax is of the values before d_scale.  Whole tiles
+    through TMA stores (macro_tile0 128 / 256), 64-wide tiles through direct stores, split-k
+    reductions; m is ragged against every tile width and its leading dimension a multiple of 16 bytes."""
+    import torch
+    m, n, k = 1008, 600, 320
+    case = gg.make_case(dt, lay, 901 + cg + bm + split, m, n, k, alpha=0.75, beta=0.0, ld_align=16)
+    A, B = gu.to_dev(case["A_bits"], dt), gu.to_dev(case["B_bits"], dt)
+    g = np.random.default_rng(6)
+    bias = g.standard_normal(m).astype(np.float32)
+    dbias = torch.from_numpy(bias).cuda()
+    d_scale = 3.5
+    W = 128 if dt == "fp8" else 64
+    sol = tl.Solution(kernel=tl.KERNEL_TCGEN05, macro_tile0=bm, macro_tile1=128 * cg, depth_u=W, stages=4,
+                      split_k=split)
+    p = tl.Problem.make(m, n, k, dtype=dt, out_dtype="fp8", trans_a=lay[0] == "T", trans_b=lay[1] == "T",
+                        alpha=0.75, lda=case["lda"], ldb=case["ldb"], kernel="tcgen05")
+    D = torch.full((m * n,), 0x7f, dtype=torch.uint8, device="cuda")
+    amax = torch.zeros(1, dtype=torch.float32, device="cuda")
+    h.gemm_ex(p, D, None, A, B, bias=dbias, activation=act, amax=amax, d_scale=d_scale, solution=sol)
+    h.device_status()
+    got = orc.e4m3_to_f32(D.cpu().numpy()).reshape(n, m).T
+    pre = _epi_ref(gu.mat(gu.oracle_ref(case), m, n, m), bias, act)       # before d_scale
+    want = orc.e4m3_to_f32(orc.f32_to_e4m3((pre * np.float32(d_scale)).astype(np.float32)))
+    # accumulation-order differences may move a value across a rounding boundary: one E4M3 step
+    mag = np.maximum(np.abs(want.astype(np.float64)), 2.0 ** -6)
+    step = 2.0 ** (np.floor(np.log2(mag)) - 3)
+    assert np.all(np.abs(got - want) <= step + 1e-12)
+    assert np.mean(got == want) > 0.99
+    assert abs(amax.item() - np.abs(pre).max()) <= 1e-4 * np.abs(pre).max()
+    # tl_gemm with an fp8 output: the same without bias and activation, d_scale 1
+    D2 = torch.zeros(m * n, dtype=torch.uint8, device="cuda")
+    h.gemm(p, D2, None, A, B, solution=sol)
+    h.device_status()
+    got2 = orc.e4m3_to_f32(D2.cpu().numpy()).reshape(n, m).T
+    want2 = orc.e4m3_to_f32(orc.f32_to_e4m3(gu.mat(gu.oracle_ref(case), m, n, m).astype(np.float32)))
+    mag2 = np.maximum(np.abs(want2.astype(np.float64)), 2.0 ** -6)
+    assert np.all(np.abs(got2 - want2) <= 2.0 ** (np.floor(np.log2(mag2)) - 3) + 1e-12)
+
+
+def test_fp8_output_refusals(h):
+    import torch
+    A = torch.zeros(128 * 128, dtype=torch.bfloat16, device="cuda")
+    D = torch.zeros(128 * 128, dtype=torch.uint8, device="cuda")
+    p = tl.Problem.make(128, 128, 128, dtype="bf16", out_dtype="fp8", beta=0.5)
+    with pytest.raises(tl.TLError) as e:
+        h.gemm(p, D, D, A, A)
+    assert e.value.status == tl.ERR_UNSUPPORTED and "beta" in str(e.value)
+    q = tl.Problem.make(128, 128, 128, dtype="bf16", out_dtype="fp8", kernel="simt")
+    with pytest.raises(tl.TLError) as e:
+        h.gemm(q, D, None, A, A)
+    assert e.value.status == tl.ERR_UNSUPPORTED
+
+
 def test_fused_epilogue_errors_and_linear(h):
     import torch
     p = tl.Problem.make(64, 64, 64, dtype="fp32")

@@ -136,7 +136,7 @@ def test_fp8_8192_per_tensor_scaling():
 def test_grouped_256_seed3_one_launch():
     import torch
     torch.cuda.init()
-    sizes = orc.grouped_sizes(3, 256)
+    _, sizes = orc.grouped_sizes(3, 256)
     assert sizes[:3] == [(1680, 880, 3840), (224, 576, 832), (416, 1040, 1408)]
     gen = torch.Generator(device="cuda").manual_seed(3)
     probs, A, B, D = [], [], [], []
