@@ -9,10 +9,16 @@ cast to bf16 (RNE), fp32 accumulation, bf16 output.  One step = one GEMM launch.
              of the inputs (4 x 128 MiB > the 129 MB L2) so no step reads the previous one's tiles
              from L2.
   e2e        the same GEMM through the public API with host buffers: per step the pinned-host A,
-             B, C are copied in (tl_memcpy_h2d), the GEMM runs, D is copied out (tl_memcpy_d2h).
+             B, C are copied in (tl_memcpy_h2d), the GEMM runs, D is copied out (tl_memcpy_d2h);
+             with the host link's own pinned bandwidth beside it (copy_bound), the rate e2e cannot beat.
   roofline   the tcgen05 kernel against the measured dense bf16 peak (MEASURED_PEAKS.json).
   cpu_baseline  the reference's CPU GEMM loop (src/gemmMfma.cpp:313-346, restated in oracle/) on
-             a bounded sample of output columns of the same problem, all host threads.
+             a bounded sample of output columns of the same problem, all host threads, and on one
+             thread as the reference runs it; the host's CPU model is named.
+  suite      (default run only) the other configurations, measured after the headline: fp16 and the
+             other bf16 layouts at 4096^3, bf16 480x1024x4096, fp8 8192^3, the 256-problem grouped
+             launch, forward+backward, bf16x3 / bf16x6 / CUDA-core fp32 at 8192^3 and the CUDA-core
+             480x512x512 case -- throughput, roofline fraction and FP64 error of each.
 
 Other workloads (--workload): fp16_4096_nn|nt|tn, bf16_4096_nt|tn, bf16_480x1024x4096, bf16x3_8192,
 simt_fp32_8192, fp8_8192, grouped256, fwdbwd.  `--impl reference` times the reference's CPU loop
@@ -193,54 +199,92 @@ def to_device_dtype(x, dtype):
 # ----------------------------------------------------------------------------------------------
 # CPU baseline: the reference loop (oracle port) on a bounded column sample
 # ----------------------------------------------------------------------------------------------
-def cpu_sample_setup(w, A, B, dtype):
-    """Packed TN storage (Ap[m][k], Bp[n][k]) of the values the GPU multiplies (fp32 widened)."""
+def cpu_sample_setup(w, A, B, dtype, C=None):
+    """Packed TN storage (Ap[m][k], Bp[n][k]) of the values the GPU multiplies, and C (column-major
+    m x n), all as fp32 (inputs rounded to the GPU dtype, then widened)."""
     import torch
     m, n, k = w["m"], w["n"], w["k"]
     ta, tb = w["lay"][0] == "T", w["lay"][1] == "T"
 
     def widen(x):
-        if dtype in ("bf16", "fp16"):
+        if x is not None and dtype in ("bf16", "fp16"):
             tt = torch.bfloat16 if dtype == "bf16" else torch.float16
             return torch.from_numpy(x).to(tt).float().numpy()
         return x
     Aw, Bw = widen(A), widen(B)
     Ap = np.ascontiguousarray(Aw.reshape(m, k) if ta else Aw.reshape(k, m).T)          # m x k
     Bp = np.ascontiguousarray(Bw.reshape(k, n).T if tb else Bw.reshape(n, k))          # n x k
-    return Ap.astype(np.float32), Bp.astype(np.float32)
+    Cw = np.ascontiguousarray(widen(C), np.float32) if C is not None else None
+    return Ap.astype(np.float32), Bp.astype(np.float32), Cw
 
 
-def cpu_run_columns(Ap, Bp, m, n, k, cols, threads, col0=0):
+def cpu_run_columns(Ap, Bp, m, n, k, cols, threads, col0=0, alpha=1.0, beta=0.0, C=None):
+    """The reference loop (alpha*sum + beta*c per element) over output columns [col0, col0 + cols)."""
     import ctypes
     from oracle import oracle as orc
     L = orc.lib()
     D = np.zeros((cols, m), np.float32)
     f32p = ctypes.POINTER(ctypes.c_float)
     Bsub = np.ascontiguousarray(Bp[col0:col0 + cols])
+    use_c = C is not None and beta != 0.0
+    Csub = np.ascontiguousarray(C[col0 * m:(col0 + cols) * m]) if use_c else None
     t0 = time.perf_counter()
-    L.orc_gemm_ref_f32_packed(m, cols, k, ctypes.c_float(1.0), Ap.ctypes.data_as(f32p), Bsub.ctypes.data_as(f32p),
+    L.orc_gemm_ref_f32_packed(m, cols, k, ctypes.c_float(alpha), Ap.ctypes.data_as(f32p), Bsub.ctypes.data_as(f32p),
+                              ctypes.c_float(beta if use_c else 0.0), Csub.ctypes.data_as(f32p) if use_c else None, m,
                               D.ctypes.data_as(f32p), m, 0, cols, threads)
     return time.perf_counter() - t0
 
 
-def cpu_baseline(w, A, B, dtype, target_s=10.0, threads=None):
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part")):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def _cpu_rate(Ap, Bp, m, n, k, threads, target_s, alpha, beta, C):
+    """(columns, seconds) of the loop on `threads` threads over a sample sized to about target_s."""
+    c0 = min(n, max(threads, 1))
+    t = cpu_run_columns(Ap, Bp, m, n, k, c0, threads, alpha=alpha, beta=beta, C=C)
+    cols = int(min(n, max(c0, c0 / max(t, 1e-6) * target_s)))
+    t = cpu_run_columns(Ap, Bp, m, n, k, cols, threads, alpha=alpha, beta=beta, C=C)
+    return cols, t
+
+
+def cpu_baseline(w, A, B, dtype, target_s=10.0, threads=None, C=None):
+    """The reference's CPU GEMM loop (cpuCompute, restated) on a bounded column sample of the same
+    problem: on all host threads (value) and on one thread, as the reference runs it."""
     from oracle import oracle as orc
     orc.lib()
     threads = threads or os.cpu_count() or 1
     m, n, k = w["m"], w["n"], w["k"]
-    Ap, Bp = cpu_sample_setup(w, A, B, dtype)
+    alpha, beta = w.get("alpha", 1.0), w.get("beta", 0.0)
+    Ap, Bp, Cw = cpu_sample_setup(w, A, B, dtype, C)
     per_col = 2.0 * m * k
-    # calibrate on a few columns, then size the sample to ~target_s
-    c0 = min(n, max(threads, 1))
-    t = cpu_run_columns(Ap, Bp, m, n, k, c0, threads)
-    rate = c0 / max(t, 1e-6)
-    cols = int(min(n, max(c0, rate * target_s)))
-    t = cpu_run_columns(Ap, Bp, m, n, k, cols, threads)
-    tflops = per_col * cols / t / 1e12
-    return {"value": tflops, "unit": "TFLOP/s", "cores": threads, "kind": "port",
-            "sample": f"reference CPU loop (src/gemmMfma.cpp:313-346 restated, -O2 -ffp-contract=off) over {cols} of "
-                      f"{n} output columns of the {m}x{n}x{k} problem, {t:.1f} s, {threads} threads",
-            "seconds": t}
+    cols, t = _cpu_rate(Ap, Bp, m, n, k, threads, target_s, alpha, beta, Cw)
+    cols1, t1 = _cpu_rate(Ap, Bp, m, n, k, 1, target_s / 3.0, alpha, beta, Cw)
+    model = cpu_model()
+    return {"value": per_col * cols / t / 1e12, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+            "cpu_model": model,
+            "sample": f"reference CPU loop (src/gemmMfma.cpp:313-346 restated, -O2 -ffp-contract=off: "
+                      f"alpha*sum + beta*c) over {cols} of {n} output columns of the {m}x{n}x{k} problem, "
+                      f"{t:.1f} s, {threads} threads ({model})",
+            "seconds": t,
+            "single_thread": {"value": per_col * cols1 / t1 / 1e12, "unit": "TFLOP/s", "cores": 1,
+                              "sample": f"{cols1} of {n} columns, {t1:.1f} s, one thread (as the reference "
+                                        f"runs cpuCompute)"}}
 
 
 # ----------------------------------------------------------------------------------------------
@@ -413,7 +457,7 @@ def run_gpu(args, w, name):
     if e2e is not None:
         line["e2e"] = e2e
     if not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(w, A, B, dtype, target_s=args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(w, A, B, dtype, target_s=args.cpu_seconds, C=C)
     h.close()
     return line
 
@@ -443,28 +487,30 @@ def describe(w, name):
 
 
 def fp64_error(h, w, A, B, C, d, out_dt, scale_a, scale_b, base):
-    """max|d - r| / max|r| with r the FP64 product of the exact operand values the GPU used."""
+    """max|d - r| / max|r| with r the FP64 product of the exact operand values the GPU used (torch
+    float64 on the device, outside the timed region), reduced on the device by tl_error_norms."""
     import torch
     import tensilelite_gb300 as tl
     m, n, k = w["m"], w["n"], w["k"]
     ta, tb = w["lay"][0] == "T", w["lay"][1] == "T"
     if w["dtype"] == "fp8":
-        def deq(q, s):
-            return q.view(torch.float8_e4m3fn).float().double().cpu().numpy() * s
-        Av, Bv = deq(base[0], scale_a), deq(base[1], scale_b)
+        Av = base[0].view(torch.float8_e4m3fn).double() * scale_a
+        Bv = base[1].view(torch.float8_e4m3fn).double() * scale_b
     else:
-        Av = base[0].double().cpu().numpy()
-        Bv = base[1].double().cpu().numpy()
-    opA = Av.reshape(m, k) if ta else Av.reshape(k, m).T
-    opB = Bv.reshape(k, n) if tb else Bv.reshape(n, k).T
+        Av, Bv = base[0].double(), base[1].double()
+    # row-major views of the column-major buffers: X stored R x C (ld R) is the (C, R) tensor X^T
+    opA = Av.view(m, k) if ta else Av.view(k, m).T
+    opB = Bv.view(k, n) if tb else Bv.view(n, k).T
     R = w["alpha"] * (opA @ opB)
+    del Av, Bv, opA, opB
     if C is not None:
         Cv = torch.from_numpy(C).to({"bf16": torch.bfloat16, "fp16": torch.float16, "fp32": torch.float32}[out_dt])
-        R = R + w["beta"] * Cv.double().numpy().reshape(n, m).T
-    Rc = torch.from_numpy(np.ascontiguousarray(R.T)).cuda()        # column-major m x n
+        R += w["beta"] * Cv.cuda().double().view(n, m).T
+    Rc = R.T.contiguous()                                             # column-major m x n
+    del R
     out = h.error_norms({"fp32": tl.FP32, "bf16": tl.BF16, "fp16": tl.FP16}[out_dt], d, m, Rc, m, m, n)
     return {"normwise": out[0] / out[1] if out[1] else out[0], "max_abs": out[0], "max_ref": out[1],
-            "reduction": "on-device FP64 (tl_error_norms); reference = numpy float64 matmul of the exact operands"}
+            "reduction": "on-device FP64 (tl_error_norms); reference = float64 product of the exact operands"}
 
 
 def run_e2e(h, p, sol, base, dC, m, n, tdt, stream, steps):
@@ -525,10 +571,62 @@ def run_e2e(h, p, sol, base, dC, m, n, tdt, stream, steps):
     ev1.synchronize()
     ms = ev0.elapsed_time(ev1)
     flops = p.flops() * steps
+    bound = copy_bound(hA, dA[0], hD[0], dD[0], s_in, s_out, bi, bo, p.flops())
     return {"value": round(flops / (ms / 1e3) / 1e12, 3), "unit": "TFLOP/s", "h2d_bytes_per_step": int(bi),
             "d2h_bytes_per_step": int(bo), "steps": steps, "ms_per_step": round(ms / steps, 4),
             "path": "pinned host -> tl_memcpy_h2d -> tl_gemm -> tl_memcpy_d2h, three streams pipelined "
-                    "(copies of step i+1 and i-1 overlap the GEMM of step i), double-buffered device operands"}
+                    "(copies of step i+1 and i-1 overlap the GEMM of step i), double-buffered device operands",
+            "copy_bound": bound}
+
+
+def copy_bound(h_in, d_in, h_out, d_out, s_in, s_out, bi, bo, flops_per_step, reps=20):
+    """The host link's own pinned bandwidth, one tl_memcpy (cudaMemcpyAsync) per copy as the e2e path
+    makes them: host->device alone, device->host alone, and both directions at once (the pipelined e2e
+    overlaps them).  An e2e step cannot beat the time its bytes take at these rates."""
+    import torch
+    import tensilelite_gb300 as tl
+    L = tl.lib()
+    nb_in = h_in.numel() * h_in.element_size()
+    nb_out = h_out.numel() * h_out.element_size()
+
+    def timed(fn, stream):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    h2d = lambda: tl.check(L.tl_memcpy_h2d(d_in.data_ptr(), h_in.data_ptr(), nb_in, s_in.cuda_stream))
+    d2h = lambda: tl.check(L.tl_memcpy_d2h(h_out.data_ptr(), d_out.data_ptr(), nb_out, s_out.cuda_stream))
+    ms_in = timed(h2d, s_in)
+    ms_out = timed(d2h, s_out)
+    # both directions at once: the two streams side by side, timed on s_in after joining s_out
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s_in)
+    s_out.wait_event(e0)
+    for _ in range(reps):
+        h2d()
+        d2h()
+    s_in.wait_stream(s_out)
+    e1.record(s_in)
+    e1.synchronize()
+    ms_both = e0.elapsed_time(e1) / reps
+    gbs_in, gbs_out = nb_in / ms_in / 1e6, nb_out / ms_out / 1e6
+    # per step: each direction at its own rate, and both together at the rate they reach side by side
+    alone_ms = max(bi / (gbs_in * 1e6), bo / (gbs_out * 1e6))
+    duplex_ms = (bi + bo) * ms_both / (nb_in + nb_out)
+    step_ms = max(alone_ms, duplex_ms)
+    return {"h2d_gbs": round(gbs_in, 1), "d2h_gbs": round(gbs_out, 1),
+            "both_directions_gbs": round((nb_in + nb_out) / ms_both / 1e6, 1),
+            "step_ms_at_link_rate": round(step_ms, 4),
+            "tflops_at_link_rate": round(flops_per_step / (step_ms / 1e3) / 1e12, 2),
+            "measured": f"{reps} copies of {nb_in >> 20} MiB host->device and {nb_out >> 20} MiB device->host from "
+                        f"pinned memory, one cudaMemcpyAsync each; alone and both directions together"}
 
 
 def grouped_sizes(seed, count):
@@ -804,30 +902,84 @@ def run_reference(args, w, name):
     dtype = w["dtype"]
     if dtype == "fp8":
         dtype = "fp32"
-    Ap, Bp = cpu_sample_setup(w, A, B, dtype)
+    Ap, Bp, Cw = cpu_sample_setup(w, A, B, dtype, C)
     m, n, k = w["m"], w["n"], w["k"]
+    alpha, beta = w.get("alpha", 1.0), w.get("beta", 0.0)
     per_col = 2.0 * m * k
     c0 = min(n, threads)
-    t = cpu_run_columns(Ap, Bp, m, n, k, c0, threads)
+    t = cpu_run_columns(Ap, Bp, m, n, k, c0, threads, alpha=alpha, beta=beta, C=Cw)
     rate = c0 / max(t, 1e-6)
     budget = min(2.0, 150.0 / max(1, args.steps + args.warmup))      # seconds per step
     cols = int(min(n, max(1, rate * budget)))
     for i in range(args.warmup):
-        cpu_run_columns(Ap, Bp, m, n, k, cols, threads, col0=(i * cols) % max(1, n - cols + 1))
+        cpu_run_columns(Ap, Bp, m, n, k, cols, threads, col0=(i * cols) % max(1, n - cols + 1), alpha=alpha,
+                        beta=beta, C=Cw)
     times = []
     for i in range(args.steps):
-        times.append(cpu_run_columns(Ap, Bp, m, n, k, cols, threads, col0=(i * cols) % max(1, n - cols + 1)))
+        times.append(cpu_run_columns(Ap, Bp, m, n, k, cols, threads, col0=(i * cols) % max(1, n - cols + 1),
+                                     alpha=alpha, beta=beta, C=Cw))
     tot = sum(times)
     value = per_col * cols * args.steps / tot / 1e12
-    sample = (f"reference CPU loop (src/gemmMfma.cpp:313-346 restated in oracle/tl_oracle.c) over {cols} of {n} "
-              f"output columns per step of the {m}x{n}x{k} problem")
+    model = cpu_model()
+    sample = (f"reference CPU loop (src/gemmMfma.cpp:313-346 restated in oracle/tl_oracle.c: alpha*sum + beta*c) "
+              f"over {cols} of {n} output columns per step of the {m}x{n}x{k} problem, {threads} threads ({model}); "
+              f"every column costs the same, so the sample's throughput stands for the whole problem")
     return {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": w["dtype"], "data": "synthetic (same seeds as the GPU arm)",
-            "config": {"workload": describe(w, name), "m": m, "n": n, "k": k, "layout": w["lay"]},
+            "config": {"workload": describe(w, name), "m": m, "n": n, "k": k, "layout": w["lay"], "alpha": alpha,
+                       "beta": beta},
             "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port", "sample": sample,
+                             "cpu_model": model},
             "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# The other benchmark configurations, measured after the headline in the same run and reported in
+# its line under "suite" (device throughput, roofline fraction, FP64 error; no e2e or CPU legs):
+# (workload, timed steps, warm-up steps)
+SUITE = [
+    ("fp16_4096_nn", 100, 10), ("bf16_4096_tn", 100, 10), ("bf16_4096_nt", 100, 10),
+    ("bf16_480x1024x4096", 2000, 20), ("fp8_8192", 50, 5), ("grouped256", 100, 5), ("fwdbwd", 200, 10),
+    ("bf16x3_8192", 20, 3), ("bf16x6_8192", 20, 3), ("simt_fp32_8192", 4, 3), ("simt_fp32_480x512x512", 2000, 20),
+]
+
+
+def compact(line):
+    """The fields of a workload's line the suite keeps."""
+    keep = {k: line.get(k) for k in ("value", "unit", "ms_per_step", "steps", "dtype", "gpu_launches")}
+    keep["workload"] = line["config"].get("workload")
+    rf = line.get("roofline", {})
+    keep["roofline"] = {k: rf.get(k) for k in ("bound", "achieved", "peak", "frac", "peak_source", "kernel_ms",
+                                               "traffic_vs_algorithmic", "note") if k in rf}
+    if "solution" in line["config"]:
+        keep["solution"] = line["config"]["solution"]
+    acc = line.get("accuracy_vs_fp64")
+    if isinstance(acc, dict) and "normwise" in acc:
+        keep["accuracy_vs_fp64"] = acc["normwise"]
+    elif acc is not None:
+        keep["accuracy_vs_fp64"] = acc
+    clk = line.get("clocks", {})
+    keep["clocks"] = {k: clk.get(k) for k in ("sm_mhz", "reasons")}
+    return keep
+
+
+def run_suite(args):
+    import torch
+    out = {}
+    for name, steps, warmup in SUITE:
+        sub = argparse.Namespace(**vars(args))
+        sub.steps, sub.warmup, sub.e2e_steps, sub.no_cpu, sub.tune = steps, warmup, 0, True, 0
+        sub.no_tune_grouped = False
+        w = WORKLOADS[name]
+        kind = w.get("kind", "gemm")
+        try:
+            line = (run_grouped if kind == "grouped" else run_fwdbwd if kind == "fwdbwd" else run_gpu)(sub, w, name)
+            out[name] = compact(line)
+        except Exception as e:                # one failing configuration does not drop the others
+            out[name] = {"error": f"{type(e).__name__}: {str(e)[:300]}"}
+        torch.cuda.empty_cache()
+    return out
 
 
 def main():
@@ -845,6 +997,9 @@ def main():
     ap.add_argument("--no-check", dest="check", action="store_false")
     ap.add_argument("--no-tune-grouped", action="store_true",
                     help="grouped256: use the plan's heuristic tile instead of tl_tune_grouped")
+    ap.add_argument("--suite", dest="suite", action="store_true", default=None,
+                    help="also measure the other configurations (default: on for the default workload)")
+    ap.add_argument("--no-suite", dest="suite", action="store_false")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
@@ -873,6 +1028,9 @@ def main():
         line = run_fwdbwd(args, w, args.workload)
     else:
         line = run_gpu(args, w, args.workload)
+    if line is not None and args.impl != "reference" and (args.suite or (args.suite is None and
+                                                                         args.workload == "bf16_4096_nn")):
+        line["suite"] = run_suite(args)
     if line is not None:
         print(json.dumps(line), flush=True)
 

@@ -76,8 +76,8 @@ def lib():
         L.orc_gemm_ref_f32.restype = ctypes.c_int
         L.orc_gemm_f64.argtypes = common + (_f64p, _i64, _i64, _i64, _i64, ctypes.c_int)
         L.orc_gemm_f64.restype = ctypes.c_int
-        L.orc_gemm_ref_f32_packed.argtypes = (_i64, _i64, _i64, ctypes.c_float, _f32p, _f32p, _f32p, _i64,
-                                              _i64, _i64, ctypes.c_int)
+        L.orc_gemm_ref_f32_packed.argtypes = (_i64, _i64, _i64, ctypes.c_float, _f32p, _f32p, ctypes.c_float,
+                                              _f32p, _i64, _f32p, _i64, _i64, _i64, ctypes.c_int)
         L.orc_gemm_ref_f32_packed.restype = ctypes.c_int
         _LIB = L
     return _LIB

@@ -377,15 +377,17 @@ ORC_API int orc_gemm_f64(int trans_a, int trans_b, int64_t M, int64_t N, int64_t
 }
 
 /* Timed form of the reference loop for the CPU baseline: runs the loop on already-packed TN storage
- * (Ap: M x K rows, Bp: N x K rows, single batch, beta = 0) over columns [n_begin, n_end).  Packing is
- * not part of the reference's cpuCompute, so it stays outside the timed call. */
+ * (Ap: M x K rows, Bp: N x K rows, single batch) over columns [n_begin, n_end), with the reference's
+ * alpha*sum + beta*C step (C column-major, ldc; NULL when beta == 0).  Packing is not part of the
+ * reference's cpuCompute, so it stays outside the timed call. */
 ORC_API int orc_gemm_ref_f32_packed(int64_t M, int64_t N, int64_t K, float alpha, const float* Ap,
-                                    const float* Bp, float* D, int64_t ldd, int64_t n_begin, int64_t n_end,
-                                    int threads)
+                                    const float* Bp, float beta, const float* C, int64_t ldc, float* D,
+                                    int64_t ldd, int64_t n_begin, int64_t n_end, int threads)
 {
     orc_job j;
     memset(&j, 0, sizeof(j));
-    j.M = M; j.N = N; j.K = K; j.batch = 1; j.alpha = alpha; j.beta = 0.0f;
+    j.M = M; j.N = N; j.K = K; j.batch = 1; j.alpha = alpha; j.beta = C ? beta : 0.0f;
+    j.C = C; j.ldc = ldc;
     j.Ap = (float*)Ap; j.Bp = (float*)Bp; j.D = D; j.ldd = ldd;
     j.n_begin = n_begin; j.n_end = n_end > N ? N : n_end;
     return run_threads(&j, run_f32, threads);
