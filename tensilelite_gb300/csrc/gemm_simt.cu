@@ -11,11 +11,14 @@
 // an outer-product step of 8 x 8 outputs is 2 + 4 shared loads and 32 packed FMAs.
 //
 // Two shapes (chosen per problem on the host):
-//   large  128 x 128 output tile, 256 threads, 8 x 8 outputs per thread, k in slabs of 8;
-//   small  64 x 32 output tile, 256 threads in 4 groups that each take a quarter of every k-slab
-//          (8 x 4 outputs per thread and group); the groups' partial tiles are summed in group order
-//          through shared memory at the end.  For problems whose 128 x 128 tiles would leave most SMs
-//          idle (the reference's 480 x 512 x 512 case: 16 large tiles, 128 small ones).
+//   large  128 x 128 output tile, 256 threads, 8 x 8 outputs per thread, k in slabs of 8, two CTAs
+//          per SM; tiles are rasterised in groups of 16 m-tiles so the tiles running together share
+//          operand rows in L2;
+//   small  64 x 32 output tile, 256 threads in 4 groups that each take a quarter of every 64-deep
+//          k-slab (8 x 4 outputs per thread and group); the groups' partial tiles are summed in group
+//          order through shared memory at the end.  For problems whose 128 x 128 tiles would leave
+//          SMs idle (the reference's 480 x 512 x 512 case: 16 large tiles, 128 small ones), one CTA
+//          per SM.
 // k-slabs are double-buffered in shared memory and prefetched into registers one slab ahead, with
 // 4-element vector loads along whichever dimension is contiguous in memory; edge tiles are
 // zero-filled on load and masked on store.  Results are deterministic (fixed summation order).
@@ -98,7 +101,10 @@ struct Cfg {
     static_assert(A_CHUNKS * THREADS * 4 == BK * BM && B_CHUNKS * THREADS * 4 == BK * BN, "whole slabs");
 };
 using CfgLarge = Cfg<128, 128, 8, 8, 1, 8, 2>;
-using CfgSmall = Cfg<64, 32, 8, 4, 4, 8, 2>;
+// one CTA per SM (it is used when tiles are fewer than SMs): up to 255 registers, 64-deep k-slabs
+using CfgSmall = Cfg<64, 32, 8, 4, 4, 16, 1>;
+
+constexpr int kRasterGroup = 16;   // m-tiles per raster group (tiles running together share B columns)
 
 template <typename TA, typename TD, typename G>
 __global__ void __launch_bounds__(G::THREADS, G::MINB) simt_gemm_kernel(const SimtParams p)
@@ -113,8 +119,15 @@ __global__ void __launch_bounds__(G::THREADS, G::MINB) simt_gemm_kernel(const Si
     const int gtid = tid % G::GT;
     const int tx = gtid % G::TX;
     const int ty = gtid / G::TX;
-    const int m_blk = blockIdx.x * BM;
-    const int n_blk = blockIdx.y * BN;
+    // raster: blocks walk groups of kRasterGroup m-tiles, m fastest, so the tiles running together
+    // share their B columns and a band of A rows in L2
+    const int tiles_m = (p.M + BM - 1) / BM, tiles_n = (p.N + BN - 1) / BN;
+    const int lin = blockIdx.x;
+    const int gsz = kRasterGroup * tiles_n;
+    const int first_m = (lin / gsz) * kRasterGroup;
+    const int gw = min(kRasterGroup, tiles_m - first_m);
+    const int m_blk = (first_m + (lin % gsz) % gw) * BM;
+    const int n_blk = ((lin % gsz) / gw) * BN;
     const int b = blockIdx.z;
     const TA* A = static_cast<const TA*>(p.A) + static_cast<int64_t>(b) * p.sa;
     const TA* B = static_cast<const TA*>(p.B) + static_cast<int64_t>(b) * p.sb;
@@ -315,9 +328,15 @@ template <typename TA, typename TD, typename G>
 tl_status launch_cfg(const SimtParams& p, int64_t M, int64_t N, int64_t batch, cudaStream_t s)
 {
     auto kern = simt_gemm_kernel<TA, TD, G>;
-    dim3 grid(static_cast<unsigned>((M + G::BM - 1) / G::BM), static_cast<unsigned>((N + G::BN - 1) / G::BN),
-              static_cast<unsigned>(batch));
-    kern<<<grid, G::THREADS, G::SMEM_BYTES, s>>>(p);          // <= 48 KB: no opt-in needed
+    if constexpr (G::SMEM_BYTES > 48 * 1024) {
+        static const cudaError_t attr =
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(G::SMEM_BYTES));
+        if (attr != cudaSuccess) return cuda_fail(attr, "cudaFuncSetAttribute(simt_gemm_kernel)");
+    }
+    const int64_t tiles = ((M + G::BM - 1) / G::BM) * ((N + G::BN - 1) / G::BN);
+    if (tiles > 0x7fffffff) return fail(TL_ERR_UNSUPPORTED, "SIMT kernel: too many tiles");
+    dim3 grid(static_cast<unsigned>(tiles), 1, static_cast<unsigned>(batch));
+    kern<<<grid, G::THREADS, G::SMEM_BYTES, s>>>(p);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "simt_gemm_kernel launch");
     return TL_SUCCESS;
@@ -367,7 +386,6 @@ tl_status simt_gemm_launch(const SimtLaunch& L, cudaStream_t s, int64_t* launche
 {
     if (L.M > 0x7fffffff || L.N > 0x7fffffff || L.K > 0x7fffffff || L.batch > 65535)
         return fail(TL_ERR_UNSUPPORTED, "SIMT kernel: dimension too large");
-    if ((L.N + 31) / 32 > 65535) return fail(TL_ERR_UNSUPPORTED, "SIMT kernel: n too large");
     tl_status st;
     switch (L.a_dtype) {
     case TL_DTYPE_FP32: st = launch_out<float>(L, s); break;
