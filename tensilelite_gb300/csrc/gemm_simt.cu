@@ -26,9 +26,14 @@
 #include <cuda_fp16.h>
 #include <cuda_fp8.h>
 
+#include <type_traits>
+
 #include "tl_internal.h"
 
 namespace tl {
+namespace tc {
+bool pdl_enabled();   // programmatic dependent launch switch, shared with the tensor-core kernel
+}
 namespace {
 
 template <typename T> __device__ __forceinline__ float to_f(T v);
@@ -81,10 +86,11 @@ struct SimtParams {
     int vec_a, vec_b;      // 4-element vector loads are aligned along the contiguous dimension
 };
 
-// Tile shape: BM x BN outputs, TM x TN per thread and k-group, KG k-groups, BKG k per group and slab.
-template <int BM_, int BN_, int TM_, int TN_, int KG_, int BKG_, int MINB_>
+// Tile shape: BM x BN outputs, TM x TN per thread and k-group, KG k-groups, BKG k per group and slab,
+// PD slabs loaded ahead into registers (1: the next slab's loads overlap one slab of FMAs; 2: two).
+template <int BM_, int BN_, int TM_, int TN_, int KG_, int BKG_, int MINB_, int PD_>
 struct Cfg {
-    static constexpr int BM = BM_, BN = BN_, TM = TM_, TN = TN_, KG = KG_, BKG = BKG_, MINB = MINB_;
+    static constexpr int BM = BM_, BN = BN_, TM = TM_, TN = TN_, KG = KG_, BKG = BKG_, MINB = MINB_, PD = PD_;
     static constexpr int TX = BM / TM;           // threads along m in a group
     static constexpr int TY = BN / TN;           // threads along n
     static constexpr int GT = TX * TY;           // threads per k-group
@@ -94,15 +100,16 @@ struct Cfg {
     static constexpr int SWN = TY * 4;
     static constexpr int A_CHUNKS = BK * BM / 4 / THREADS;   // 4-element loads per thread and slab
     static constexpr int B_CHUNKS = BK * BN / 4 / THREADS;
-    static constexpr int SMEM_FLOATS = 2 * BK * BM + 2 * BK * 2 * BN;
+    static constexpr int SMEM_FLOATS = 2 * BK * BM + 2 * BK * BN;
     static constexpr int RED_FLOATS = KG > 1 ? KG * BM * BN : 0;
     static constexpr size_t SMEM_BYTES = sizeof(float) * (SMEM_FLOATS > RED_FLOATS ? SMEM_FLOATS : RED_FLOATS);
     static_assert(TM % 4 == 0 && TN % 4 == 0, "per-thread tiles are strips of 4");
     static_assert(A_CHUNKS * THREADS * 4 == BK * BM && B_CHUNKS * THREADS * 4 == BK * BN, "whole slabs");
 };
-using CfgLarge = Cfg<128, 128, 8, 8, 1, 8, 2>;
-// one CTA per SM (it is used when tiles are fewer than SMs): up to 255 registers, 64-deep k-slabs
-using CfgSmall = Cfg<64, 32, 8, 4, 4, 16, 1>;
+using CfgLarge = Cfg<128, 128, 8, 8, 1, 8, 2, 1>;
+// one CTA per SM (it is used when tiles are fewer than SMs): up to 255 registers, 64-deep k-slabs,
+// loads two slabs ahead (eight warps per SM cannot hide a DRAM round trip behind one slab)
+using CfgSmall = Cfg<64, 32, 8, 4, 4, 16, 1, 2>;
 
 constexpr int kRasterGroup = 16;   // m-tiles per raster group (tiles running together share B columns)
 
@@ -112,7 +119,7 @@ __global__ void __launch_bounds__(G::THREADS, G::MINB) simt_gemm_kernel(const Si
     constexpr int BM = G::BM, BN = G::BN, BK = G::BK, TM = G::TM, TN = G::TN;
     extern __shared__ __align__(16) float smem[];
     float* As = smem;                        // [2][BK][BM]      op(A)(m, k) at [k][m]
-    float* Bs = smem + 2 * BK * BM;          // [2][BK][2 * BN]  op(B)(k, n) at [k][2n] and [k][2n + 1]
+    float* Bs = smem + 2 * BK * BM;          // [2][BK][BN]      op(B)(k, n) at [k][n]
 
     const int tid = threadIdx.x;
     const int grp = tid / G::GT;             // k-group
@@ -129,12 +136,18 @@ __global__ void __launch_bounds__(G::THREADS, G::MINB) simt_gemm_kernel(const Si
     const int m_blk = (first_m + (lin % gsz) % gw) * BM;
     const int n_blk = ((lin % gsz) / gw) * BN;
     const int b = blockIdx.z;
+    // Launched as a programmatic dependent: wait for the previous grid in the stream to complete
+    // (its writes visible) before the first global access, then let the next grid get scheduled.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const TA* A = static_cast<const TA*>(p.A) + static_cast<int64_t>(b) * p.sa;
     const TA* B = static_cast<const TA*>(p.B) + static_cast<int64_t>(b) * p.sb;
 
-    // ---- global -> registers (one slab ahead) -> shared
-    float4 ra[G::A_CHUNKS], rb[G::B_CHUNKS];
-    auto load_slab = [&](int k0) {
+    // ---- global -> registers (PD slabs ahead) -> shared; register set r holds the slabs s with
+    // s % PD == r (indexes are compile-time constants after inlining)
+    float4 ra[G::PD][G::A_CHUNKS], rb[G::PD][G::B_CHUNKS];
+    auto load_slab = [&](auto rset, int k0) {
+        constexpr int r = decltype(rset)::value;
 #pragma unroll
         for (int c = 0; c < G::A_CHUNKS; ++c) {
             const int idx = tid + c * G::THREADS;
@@ -164,7 +177,7 @@ __global__ void __launch_bounds__(G::THREADS, G::MINB) simt_gemm_kernel(const Si
                     }
                 }
             }
-            ra[c] = v;
+            ra[r][c] = v;
         }
 #pragma unroll
         for (int c = 0; c < G::B_CHUNKS; ++c) {
@@ -195,24 +208,25 @@ __global__ void __launch_bounds__(G::THREADS, G::MINB) simt_gemm_kernel(const Si
                     }
                 }
             }
-            rb[c] = v;
+            rb[r][c] = v;
         }
     };
-    auto store_slab = [&](int buf) {
+    auto store_slab = [&](auto rset, int buf) {
+        constexpr int r = decltype(rset)::value;
         float* as = As + buf * BK * BM;
-        float* bs = Bs + buf * BK * 2 * BN;
+        float* bs = Bs + buf * BK * BN;
 #pragma unroll
         for (int c = 0; c < G::A_CHUNKS; ++c) {
             const int idx = tid + c * G::THREADS;
             if (!p.trans_a) {
                 const int m = (idx % (BM / 4)) * 4, k = idx / (BM / 4);
-                *reinterpret_cast<float4*>(as + k * BM + m) = ra[c];
+                *reinterpret_cast<float4*>(as + k * BM + m) = ra[r][c];
             } else {
                 const int m = idx % BM, k = (idx / BM) * 4;
-                as[(k + 0) * BM + m] = ra[c].x;
-                as[(k + 1) * BM + m] = ra[c].y;
-                as[(k + 2) * BM + m] = ra[c].z;
-                as[(k + 3) * BM + m] = ra[c].w;
+                as[(k + 0) * BM + m] = ra[r][c].x;
+                as[(k + 1) * BM + m] = ra[r][c].y;
+                as[(k + 2) * BM + m] = ra[r][c].z;
+                as[(k + 3) * BM + m] = ra[r][c].w;
             }
         }
 #pragma unroll
@@ -220,15 +234,14 @@ __global__ void __launch_bounds__(G::THREADS, G::MINB) simt_gemm_kernel(const Si
             const int idx = tid + c * G::THREADS;
             if (p.trans_b) {
                 const int n = (idx % (BN / 4)) * 4, k = idx / (BN / 4);
-                float* row = bs + k * 2 * BN + 2 * n;
-                *reinterpret_cast<float4*>(row) = make_float4(rb[c].x, rb[c].x, rb[c].y, rb[c].y);
-                *reinterpret_cast<float4*>(row + 4) = make_float4(rb[c].z, rb[c].z, rb[c].w, rb[c].w);
+                *reinterpret_cast<float4*>(bs + k * BN + n) = rb[r][c];
             } else {
                 const int n = idx % BN, k = (idx / BN) * 4;
-                *reinterpret_cast<float2*>(bs + (k + 0) * 2 * BN + 2 * n) = make_float2(rb[c].x, rb[c].x);
-                *reinterpret_cast<float2*>(bs + (k + 1) * 2 * BN + 2 * n) = make_float2(rb[c].y, rb[c].y);
-                *reinterpret_cast<float2*>(bs + (k + 2) * 2 * BN + 2 * n) = make_float2(rb[c].z, rb[c].z);
-                *reinterpret_cast<float2*>(bs + (k + 3) * 2 * BN + 2 * n) = make_float2(rb[c].w, rb[c].w);
+                const float4 q = rb[r][c];
+                bs[(k + 0) * BN + n] = q.x;
+                bs[(k + 1) * BN + n] = q.y;
+                bs[(k + 2) * BN + n] = q.z;
+                bs[(k + 3) * BN + n] = q.w;
             }
         }
     };
@@ -241,17 +254,9 @@ __global__ void __launch_bounds__(G::THREADS, G::MINB) simt_gemm_kernel(const Si
 #pragma unroll
         for (int j = 0; j < TN; ++j) acc[i][j] = make_float2(0.f, 0.f);
 
-    const int nslab = (p.K + BK - 1) / BK;
-    if (nslab > 0) {
-        load_slab(0);
-        store_slab(0);
-    }
-    __syncthreads();
-    for (int s = 0; s < nslab; ++s) {
-        const int buf = s & 1;
-        if (s + 1 < nslab) load_slab((s + 1) * BK);
+    auto compute_slab = [&](int buf) {
         const float* as = As + buf * BK * BM + grp * G::BKG * BM;
-        const float* bs = Bs + buf * BK * 2 * BN + grp * G::BKG * 2 * BN;
+        const float* bs = Bs + buf * BK * BN + grp * G::BKG * BN;
 #pragma unroll
         for (int kk = 0; kk < G::BKG; ++kk) {
             float2 a[TM / 2], bd[TN];
@@ -263,21 +268,52 @@ __global__ void __launch_bounds__(G::THREADS, G::MINB) simt_gemm_kernel(const Si
             }
 #pragma unroll
             for (int st = 0; st < TN / 4; ++st) {
-                const float* row = bs + kk * 2 * BN + 2 * (st * G::SWN + ty * 4);
-                const float4 v0 = *reinterpret_cast<const float4*>(row);
-                const float4 v1 = *reinterpret_cast<const float4*>(row + 4);
-                bd[4 * st + 0] = make_float2(v0.x, v0.y);
-                bd[4 * st + 1] = make_float2(v0.z, v0.w);
-                bd[4 * st + 2] = make_float2(v1.x, v1.y);
-                bd[4 * st + 3] = make_float2(v1.z, v1.w);
+                const float4 v = *reinterpret_cast<const float4*>(bs + kk * BN + st * G::SWN + ty * 4);
+                bd[4 * st + 0] = make_float2(v.x, v.x);
+                bd[4 * st + 1] = make_float2(v.y, v.y);
+                bd[4 * st + 2] = make_float2(v.z, v.z);
+                bd[4 * st + 3] = make_float2(v.w, v.w);
             }
 #pragma unroll
             for (int i = 0; i < TM / 2; ++i)
 #pragma unroll
                 for (int j = 0; j < TN; ++j) acc[i][j] = __ffma2_rn(a[i], bd[j], acc[i][j]);
         }
-        if (s + 1 < nslab) store_slab(buf ^ 1);
+    };
+    using R0 = std::integral_constant<int, 0>;
+    using R1 = std::integral_constant<int, G::PD - 1>;
+    const int nslab = (p.K + BK - 1) / BK;
+    if (nslab > 0) {
+        load_slab(R0{}, 0);
+        store_slab(R0{}, 0);
+    }
+    if constexpr (G::PD == 1) {
         __syncthreads();
+        for (int s = 0; s < nslab; ++s) {
+            const int buf = s & 1;
+            if (s + 1 < nslab) load_slab(R0{}, (s + 1) * BK);
+            compute_slab(buf);
+            if (s + 1 < nslab) store_slab(R0{}, buf ^ 1);
+            __syncthreads();
+        }
+    } else {
+        // slab s is computed from shared buffer s & 1 while slab s + 2 is loaded into register set
+        // s & 1 (slab s went from that set to shared memory a step earlier) and slab s + 1 moves
+        // from register set (s + 1) & 1 into the other shared buffer
+        if (nslab > 1) load_slab(R1{}, BK);
+        __syncthreads();
+        auto step = [&](auto rset, int s) {
+            constexpr int r = decltype(rset)::value;
+            using RN = std::integral_constant<int, r ^ 1>;
+            if (s + 2 < nslab) load_slab(rset, (s + 2) * BK);
+            compute_slab(r);
+            if (s + 1 < nslab) store_slab(RN{}, r ^ 1);
+            __syncthreads();
+        };
+        for (int s = 0; s < nslab; s += 2) {
+            step(R0{}, s);
+            if (s + 1 < nslab) step(R1{}, s + 1);
+        }
     }
 
     // ---- epilogue: D = alpha*acc + beta*C (C not read when beta == 0)
@@ -335,10 +371,20 @@ tl_status launch_cfg(const SimtParams& p, int64_t M, int64_t N, int64_t batch, c
     }
     const int64_t tiles = ((M + G::BM - 1) / G::BM) * ((N + G::BN - 1) / G::BN);
     if (tiles > 0x7fffffff) return fail(TL_ERR_UNSUPPORTED, "SIMT kernel: too many tiles");
-    dim3 grid(static_cast<unsigned>(tiles), 1, static_cast<unsigned>(batch));
-    kern<<<grid, G::THREADS, G::SMEM_BYTES, s>>>(p);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "simt_gemm_kernel launch");
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(static_cast<unsigned>(tiles), 1, static_cast<unsigned>(batch));
+    cfg.blockDim = dim3(G::THREADS, 1, 1);
+    cfg.dynamicSmemBytes = G::SMEM_BYTES;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    if (tc::pdl_enabled()) {
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+    }
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, p);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchKernelEx(simt_gemm_kernel)");
     return TL_SUCCESS;
 }
 
