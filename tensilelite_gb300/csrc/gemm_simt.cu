@@ -106,10 +106,10 @@ struct Cfg {
     static_assert(TM % 4 == 0 && TN % 4 == 0, "per-thread tiles are strips of 4");
     static_assert(A_CHUNKS * THREADS * 4 == BK * BM && B_CHUNKS * THREADS * 4 == BK * BN, "whole slabs");
 };
-using CfgLarge = Cfg<128, 128, 8, 8, 1, 8, 2, 1>;
+using CfgLarge = Cfg<128, 128, 16, 8, 1, 8, 2, 1>;
 // one CTA per SM (it is used when tiles are fewer than SMs): up to 255 registers, 64-deep k-slabs,
 // loads two slabs ahead (eight warps per SM cannot hide a DRAM round trip behind one slab)
-using CfgSmall = Cfg<64, 32, 8, 4, 4, 16, 1, 2>;
+using CfgSmall = Cfg<64, 32, 8, 8, 8, 8, 1, 2>;
 
 constexpr int kRasterGroup = 16;   // m-tiles per raster group (tiles running together share B columns)
 
