@@ -6,22 +6,27 @@
 //
 // Blackwell issues two fp32 FMAs per instruction (fma.rn.f32x2, __ffma2_rn): each thread keeps its
 // TM x TN accumulators as float2 pairs along m, and one packed FMA multiplies a pair of A values by
-// a B value held twice ({b, b}).  The B tile is therefore stored in shared memory with every value
-// duplicated, so the pairs come straight out of 16-byte shared loads with no packing instructions;
-// an outer-product step of 8 x 8 outputs is 2 + 4 shared loads and 32 packed FMAs.
+// a B value held twice ({b, b}, formed in registers).  What bounds a CUDA-core GEMM on this SM is the
+// shared-memory read path rather than the FMA pipes: a 16-byte shared load delivers 4 floats per
+// thread over four cycles whatever the broadcast, so the SM reads at most 32 floats per cycle while
+// its FMA pipes retire 128 FMAs.  A thread's outer-product step of TM x TN FMAs reads TM + TN
+// floats, so the tiles per thread are as large as the registers allow: 16 x 8 (128 FMAs per 24
+// floats, the shared path 75 % busy when the pipes are full).  B is stored once (not duplicated),
+// which halves its shared reads at the cost of forming the {b, b} pairs in registers (issue slots
+// are free: a packed FMA holds the pipe two cycles).
 //
 // Two shapes (chosen per problem on the host):
-//   large  128 x 128 output tile, 256 threads, 8 x 8 outputs per thread, k in slabs of 8, two CTAs
-//          per SM; tiles are rasterised in groups of 16 m-tiles so the tiles running together share
-//          operand rows in L2;
-//   small  64 x 32 output tile, 256 threads in 4 groups that each take a quarter of every 64-deep
-//          k-slab (8 x 4 outputs per thread and group); the groups' partial tiles are summed in group
-//          order through shared memory at the end.  For problems whose 128 x 128 tiles would leave
-//          SMs idle (the reference's 480 x 512 x 512 case: 16 large tiles, 128 small ones), one CTA
-//          per SM.
-// k-slabs are double-buffered in shared memory and prefetched into registers one slab ahead, with
-// 4-element vector loads along whichever dimension is contiguous in memory; edge tiles are
-// zero-filled on load and masked on store.  Results are deterministic (fixed summation order).
+//   large  128 x 128 output tile, 128 threads, 16 x 8 outputs per thread, k in slabs of 8, two
+//          CTAs per SM; tiles are rasterised in groups of 16 m-tiles so the tiles running together
+//          share operand rows in L2;
+//   small  64 x 32 output tile, 256 threads in 8 groups that each take an eighth of every 64-deep
+//          k-slab (8 x 8 outputs per thread and group); the groups' partial tiles are summed in
+//          group order through shared memory at the end.  For problems whose 128 x 128 tiles would
+//          leave SMs idle (the reference's 480 x 512 x 512 case: 16 large tiles, 128 small ones),
+//          one CTA per SM, slabs loaded two ahead.
+// k-slabs are double-buffered in shared memory and prefetched into registers, with 4-element vector
+// loads along whichever dimension is contiguous in memory; edge tiles are zero-filled on load and
+// masked on store.  Results are deterministic (fixed summation order).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_fp8.h>
