@@ -401,6 +401,35 @@ TL_API tl_status tl_device_status(tl_handle* handle, void* stream);
 /* Limit of every device-side wait, in milliseconds (default 4000; also env TL_WAIT_TIMEOUT_MS). */
 TL_API tl_status tl_set_wait_timeout(tl_handle* handle, uint32_t ms);
 
+/* Device timeline of the tensor-core kernel, the counterpart of the reference's per-wave thread
+ * trace (test/ttrace, read with s_memtime stamps in its kernels).  While a buffer is set, every
+ * tensor-core GEMM launched through the handle writes, for each CTA, TL_TRACE_SLOTS 64-bit words
+ * at [cta * TL_TRACE_SLOTS]: the SM cycle counter (%clock64) at the events below, for the CTA's
+ * first tile, plus the global nanosecond timer at entry and exit and the SM id.  A launch whose
+ * grid needs more words than `bytes` holds records nothing.  NULL (or 0 bytes) switches it off.
+ * The buffer is device memory the caller owns; slots of events a CTA does not reach are left as
+ * they were (fill the buffer with zeros first). */
+#define TL_TRACE_SLOTS 16
+enum {
+    TL_TRACE_ENTRY = 0,        /* kernel entry */
+    TL_TRACE_ENTRY_NS = 1,     /* %globaltimer at entry */
+    TL_TRACE_SETUP = 2,        /* barriers initialised, TMEM allocated, CTAs of the cluster in step */
+    TL_TRACE_DEP = 3,          /* the previous grid in the stream has completed (programmatic launch) */
+    TL_TRACE_LOAD_FIRST = 4,   /* producer: first tile's first TMA load issued */
+    TL_TRACE_LOAD_LAST = 5,    /* producer: first tile's last TMA load issued */
+    TL_TRACE_MMA_FIRST = 6,    /* MMA warp: first tile's first stage landed */
+    TL_TRACE_MMA_LAST = 7,     /* MMA warp: first tile's last MMA committed */
+    TL_TRACE_ACC_READY = 8,    /* epilogue: first tile's accumulator ready */
+    TL_TRACE_STORED = 9,       /* epilogue: first tile's output (or split-k partial) written */
+    TL_TRACE_REDUCED = 10,     /* epilogue: split-k reduction of the first tile finished */
+    TL_TRACE_EPI_END = 11,     /* epilogue: every tile done */
+    TL_TRACE_EXIT = 12,        /* TMEM released, CTA about to exit */
+    TL_TRACE_EXIT_NS = 13,     /* %globaltimer at exit */
+    TL_TRACE_SMID = 14,        /* the SM the CTA ran on */
+    TL_TRACE_TILES = 15        /* work units the CTA processed */
+};
+TL_API tl_status tl_set_trace(tl_handle* handle, void* device_buffer, int64_t bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,6 +34,10 @@ OP_N, OP_T = 0, 1
 KERNEL_AUTO, KERNEL_SIMT, KERNEL_TCGEN05, KERNEL_BF16X3, KERNEL_BF16X6 = 0, 1, 2, 3, 4
 ROUND_RNE, ROUND_TRUNCATE = 0, 1
 DEBUG_SKIP_LOADS = 1   # tl_gemm_solution.debug_flags: the producer issues no copies (timeout-path tests)
+# device timeline (Handle.set_trace): words per CTA and their events (include/tensilelite.h)
+TRACE_SLOTS = 16
+TRACE_EVENTS = ("entry", "entry_ns", "setup", "dep", "load_first", "load_last", "mma_first", "mma_last",
+                "acc_ready", "stored", "reduced", "epi_end", "exit", "exit_ns", "smid", "tiles")
 
 DTYPE_BYTES = {FP32: 4, FP16: 2, BF16: 2, FP8: 1}
 DTYPE_NAMES = {"fp32": FP32, "fp16": FP16, "bf16": BF16, "fp8": FP8, "fp8_e4m3": FP8}
@@ -170,6 +174,7 @@ def lib():
         "tl_tensile_launch": [_vp, ctypes.c_char_p, _vp, ctypes.c_size_t, _vp],
         "tl_kernel_timing": [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(i64), i32],
         "tl_set_wait_timeout": [_vp, ctypes.c_uint32],
+        "tl_set_trace": [_vp, _vp, ctypes.c_int64],
         "tl_gemm_noalloc": [P, S, _vp, _vp, _vp, _vp, _vp],
         "tl_noalloc_status": [_vp],
     }
@@ -355,6 +360,14 @@ class Handle:
 
     def set_wait_timeout(self, ms):
         check(lib().tl_set_wait_timeout(self._h, ms))
+
+    def set_trace(self, buffer=None):
+        """Device timeline of the tensor-core kernel (tl_set_trace): `buffer` is an int64 device tensor
+        of at least grid x TRACE_SLOTS elements, or None to switch it off."""
+        if buffer is None:
+            check(lib().tl_set_trace(self._h, None, 0))
+        else:
+            check(lib().tl_set_trace(self._h, _ptr(buffer), buffer.numel() * buffer.element_size()))
 
     # ---- grouped ----
     def grouped_plan(self, problems: Sequence[Problem], D, C, A, B, solution: Optional[Solution] = None):

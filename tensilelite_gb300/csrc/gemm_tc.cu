@@ -165,15 +165,24 @@ int persistent_workers(int in_dtype, int out_dtype, int cl, int ctas, int sm_cou
 }
 
 // Grid: one CTA per SM (cl 1) or as many co-resident clusters as fit, never more than the work.
-tl_status dispatch(int in_dtype, int out_dtype, int cl, const TcKernelParams& kp, int ctas, int sm_count,
-                   int64_t total_work, size_t smem, cudaStream_t s)
+tl_status dispatch(int in_dtype, int out_dtype, int cl, const TcKernelParams& kp_in, int ctas, int sm_count,
+                   int64_t total_work, size_t smem, cudaStream_t s, int64_t trace_bytes)
 {
     int workers = persistent_workers(in_dtype, out_dtype, cl, ctas, sm_count, smem);
     if (workers > total_work) workers = static_cast<int>(total_work);
     if (workers < 1) workers = 1;
-    if (cl == 1) return dispatch_cl<1>(in_dtype, out_dtype, kp, workers, smem, s);
-    if (cl == 2) return dispatch_cl<2>(in_dtype, out_dtype, kp, 2 * workers, smem, s);
-    return dispatch_cl<4>(in_dtype, out_dtype, kp, 4 * workers, smem, s);
+    const int grid = (cl == 1 ? 1 : (cl == 2 ? 2 : 4)) * workers;
+    const TcKernelParams* kp = &kp_in;
+    TcKernelParams untraced;
+    if (kp_in.trace != nullptr &&
+        static_cast<int64_t>(grid) * TL_TRACE_SLOTS * static_cast<int64_t>(sizeof(unsigned long long)) > trace_bytes) {
+        untraced = kp_in;             // the timeline buffer cannot hold this grid: record nothing
+        untraced.trace = nullptr;
+        kp = &untraced;
+    }
+    if (cl == 1) return dispatch_cl<1>(in_dtype, out_dtype, *kp, grid, smem, s);
+    if (cl == 2) return dispatch_cl<2>(in_dtype, out_dtype, *kp, grid, smem, s);
+    return dispatch_cl<4>(in_dtype, out_dtype, *kp, grid, smem, s);
 }
 
 uint32_t make_idesc(int in_dtype, int n_mn_major, int m_mn_major, int bm, int cg)
@@ -431,7 +440,8 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     kp.err = L.err;
     kp.timeout_ns = L.timeout_ns;
     kp.debug_skip_loads = (L.debug_flags & TL_DEBUG_SKIP_LOADS) ? 1 : 0;
-    st = dispatch(L.in_dtype, L.out_dtype, cg, kp, L.ctas, L.sm_count, kp.total_work, smem, stream);
+    kp.trace = L.trace;
+    st = dispatch(L.in_dtype, L.out_dtype, cg, kp, L.ctas, L.sm_count, kp.total_work, smem, stream, L.trace_bytes);
     if (st == TL_SUCCESS && launches) ++*launches;
     return st;
 }
@@ -466,7 +476,7 @@ tl_status tc_grouped_launch(const TcGroupLaunch& G, cudaStream_t stream, int64_t
     kp.err = G.err;
     kp.timeout_ns = G.timeout_ns;
     const size_t smem = tc_smem_bytes(G.bm / cta_group, G.stages);
-    tl_status st = dispatch(G.in_dtype, G.out_dtype, cg, kp, G.ctas, G.sm_count, G.total_tiles, smem, stream);
+    tl_status st = dispatch(G.in_dtype, G.out_dtype, cg, kp, G.ctas, G.sm_count, G.total_tiles, smem, stream, 0);
     if (st == TL_SUCCESS && launches) ++*launches;
     return st;
 }

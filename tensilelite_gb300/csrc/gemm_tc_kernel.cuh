@@ -69,7 +69,28 @@ struct TcKernelParams {
     int* err;
     unsigned long long timeout_ns;
     int debug_skip_loads;         // TL_DEBUG_SKIP_LOADS: the producer issues no copies (timeout-path test)
+    unsigned long long* trace;    // device timeline, TL_TRACE_SLOTS words per CTA, or null
 };
+
+// Timeline stamp of event `slot` for this CTA (tl_set_trace): the SM cycle counter.
+__device__ __forceinline__ void trace_mark(const TcKernelParams& p, int slot)
+{
+    if (p.trace != nullptr) {
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%clock64;" : "=l"(t) :: "memory");
+        p.trace[static_cast<size_t>(blockIdx.x) * TL_TRACE_SLOTS + slot] = t;
+    }
+}
+__device__ __forceinline__ void trace_put(const TcKernelParams& p, int slot, unsigned long long v)
+{
+    if (p.trace != nullptr) p.trace[static_cast<size_t>(blockIdx.x) * TL_TRACE_SLOTS + slot] = v;
+}
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t) :: "memory");
+    return t;
+}
 
 struct TileJob {
     const void* tmN;
@@ -759,6 +780,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
     // have released it (each slot's empty barrier expects one commit from each pair's leader).
     constexpr int CG = CL >= 2 ? 2 : 1;         // CTAs per MMA (cta_group)
     constexpr int MC = CL / CG;                 // pairs sharing the m-side operand
+    if (threadIdx.x == 0 && p.trace != nullptr) {
+        trace_mark(p, TL_TRACE_ENTRY);
+        trace_put(p, TL_TRACE_ENTRY_NS, global_ns());
+        unsigned int smid;
+        asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+        trace_put(p, TL_TRACE_SMID, smid);
+    }
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const uint32_t bmc = static_cast<uint32_t>(p.bm) / CG;            // m-side rows staged by this CTA
@@ -827,12 +855,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
     if constexpr (CL > 1) ptx::cluster_sync();     // peer barriers initialised before any remote arrive
     ptx::tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
+    if (threadIdx.x == 0) trace_mark(p, TL_TRACE_SETUP);
     // Launched as a programmatic dependent: everything above (barrier set-up, TMEM allocation,
     // descriptor prefetch) may have run while the previous kernel in the stream was finishing.
     // Wait for that grid to complete (its writes visible) before touching global memory, then let
     // the next dependent grid start its own set-up as soon as SMs free up.
     ptx::grid_dep_wait();
     ptx::grid_dep_launch_dependents();
+    if (threadIdx.x == 0) trace_mark(p, TL_TRACE_DEP);
     const int nvirt = p.nterms;
     const uint64_t tlim = p.timeout_ns;
 
@@ -924,6 +954,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         }
                     }
                     __syncwarp();
+                    if (w == unit0 && lane == 0 && (i == 0 || i == total - 1))
+                        trace_mark(p, i == 0 ? TL_TRACE_LOAD_FIRST : TL_TRACE_LOAD_LAST);
                     if (++stage == static_cast<uint32_t>(nstages)) {
                         stage = 0;
                         phase ^= 1u;
@@ -985,6 +1017,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         break;
                     }
                     ptx::tc_fence_after();
+                    if (i == 0 && w == unit0 && lane == 0) trace_mark(p, TL_TRACE_MMA_FIRST);
                     const bool is_main = !sep_small || v == nvirt - 1;
                     const uint32_t d_tmem = tmem_base + (is_main ? mbuf * bmu : (2u + sbuf) * bmu);
                     const bool started = is_main ? main_started : small_started;
@@ -1050,6 +1083,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                     }
                 }
                 __syncwarp();
+                if (w == unit0 && lane == 0) trace_mark(p, TL_TRACE_MMA_LAST);
                 if (nkb > 0) {
                     mbuf ^= 1u;
                     if (mbuf == 0) mph ^= 1u;
@@ -1073,11 +1107,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
         const int chunks = p.bm / 32;
         bool ok = true;
         float amax = 0.0f;                        // fused epilogue: this thread's max |output|
+        unsigned long long units_done = 0;
         for (int64_t w = unit0; w < p.total_work; w += units) {
             const int4 u = load_unit(p, w);      // the epilogue trails the MMAs: no need to load ahead
             TileJob j;
             get_job(p, w, u, j);
             if (j.kb1 <= j.kb0) continue;             // an empty unit of a balanced split
+            ++units_done;
+            const bool tr = (et == 0 && w == unit0);  // timeline stamps: the first tile, one thread
             j.n0 += static_cast<int>(rank) * kTcTileN;
             j.slot = j.slot * CL + rank;              // split-k slabs and counters per CTA
             const int n = j.n0 + row;
@@ -1145,6 +1182,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                     sbuf ^= 1u;
                     if (sbuf == 0) sph ^= 1u;
                 }
+                if (tr) trace_mark(p, TL_TRACE_ACC_READY);
                 if (j.nsplit == 1) {
 #pragma unroll
                     for (int q = 0; q < 4; ++q) {
@@ -1156,6 +1194,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                             store_chunk<TD, EPI>(p, amax, j, base_c, base_d, m, v, p.out_trunc);
                         }
                     }
+                    if (tr) trace_mark(p, TL_TRACE_STORED);
                 } else {
                     float* slab = p.ws + (static_cast<size_t>(j.slot) * p.tail_split + j.split) *
                                              (static_cast<size_t>(kTcTileN) * p.bm);
@@ -1167,7 +1206,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                             for (int i = 0; i < 32; ++i) __stcg(dst + i * kTcTileN, run[q * 32 + i]);
                         }
                     }
+                    if (tr) trace_mark(p, TL_TRACE_STORED);
                     split_finish<TD, EPI>(p, amax, j, ok, et, row, row_ok, base_c, base_d, last_flag);
+                    if (tr) trace_mark(p, TL_TRACE_REDUCED);
                 }
                 continue;
             }
@@ -1180,6 +1221,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             }
             const uint32_t tbase = tmem_base + lane_off + mbuf * static_cast<uint32_t>(p.bm);
             if (ok) ptx::tc_fence_after();
+            if (tr) trace_mark(p, TL_TRACE_ACC_READY);
             // A staged TMA store costs a round trip per 32 rows (the one 4 KB buffer per warp is
             // refilled only after the previous store has read it): hidden behind the next tile's
             // main loop, but exposed on a CTA's last tile, which uses the direct stores instead
@@ -1222,6 +1264,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         ptx::bulk_commit();
                     }
                 }
+                if (tr) trace_mark(p, TL_TRACE_STORED);
             } else if (j.nsplit == 1) {
                 // output TMA cannot address (unaligned D): 16-byte vector stores per thread
                 for (int c = 0; c < chunks && ok; ++c) {
@@ -1237,6 +1280,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         store_chunk<TD, EPI>(p, amax, j, base_c, base_d, m, v, p.out_trunc);
                     }
                 }
+                if (tr) trace_mark(p, TL_TRACE_STORED);
             } else {
                 // split-k: park this split's partial tile, layout [chunk][column][row] (coalesced)
                 float* slab = p.ws + (static_cast<size_t>(j.slot) * p.tail_split + j.split) *
@@ -1249,15 +1293,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
 #pragma unroll
                     for (int i = 0; i < 32; ++i) __stcg(dst + i * kTcTileN, __uint_as_float(r[i]));
                 }
+                if (tr) trace_mark(p, TL_TRACE_STORED);
                 if (p.par_reduce)
                     split_finish_parallel<TD, CG, EPI>(p, amax, j, ok, et, lane, row, row_ok, base_c, base_d, last_flag,
                                                   &tempty[mbuf], abort_flag);
                 else
                     split_finish_tmem<TD, CG, EPI>(p, amax, j, ok, et, lane, row, row_ok, base_c, base_d, last_flag, tbase,
                                               &tempty[mbuf]);
+                if (tr) trace_mark(p, TL_TRACE_REDUCED);
             }
             mbuf ^= 1u;
             if (mbuf == 0) mph ^= 1u;
+        }
+        if (et == 0) {
+            trace_mark(p, TL_TRACE_EPI_END);
+            trace_put(p, TL_TRACE_TILES, units_done);
         }
         if constexpr (EPI) {
             if (p.epi_amax != nullptr) {
@@ -1277,6 +1327,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
         ptx::tc_fence_after();
         if constexpr (CG == 2) ptx::tmem_dealloc_pair(tmem_base, tmem_cols);
         else ptx::tmem_dealloc(tmem_base, tmem_cols);
+        if (lane == 0 && p.trace != nullptr) {
+            trace_mark(p, TL_TRACE_EXIT);
+            trace_put(p, TL_TRACE_EXIT_NS, global_ns());
+        }
     }
 }
 

@@ -36,6 +36,8 @@ struct tl_handle {
     size_t counters_len = 0;
     int64_t launches = 0;
     uint64_t timeout_ns = 4000000000ull;
+    unsigned long long* trace = nullptr;   // device timeline buffer (tl_set_trace), or null
+    int64_t trace_bytes = 0;
     std::map<std::string, tl_gemm_solution> tuned;
     std::mutex mu;
     // Once a stream capture has recorded this handle's workspace address, a grown workspace retires
@@ -742,6 +744,8 @@ tl_status enqueue(tl_handle* h, const Prepared& P, cudaStream_t s)
     L.cg = P.s.macro_tile1 / kTcTileN;
     L.err = h->d_err;
     L.timeout_ns = h->timeout_ns;
+    L.trace = h->trace;
+    L.trace_bytes = h->trace_bytes;
     L.workspace = P.ws_partials;
     L.workspace_bytes = P.part_bytes;
     L.counters = h->counters;
@@ -1902,6 +1906,16 @@ TL_API tl_status tl_set_wait_timeout(tl_handle* h, uint32_t ms)
 {
     if (!h || ms == 0) return fail(TL_ERR_INVALID_ARG, "bad argument");
     h->timeout_ns = static_cast<uint64_t>(ms) * 1000000ull;
+    return TL_SUCCESS;
+}
+
+TL_API tl_status tl_set_trace(tl_handle* h, void* buf, int64_t bytes)
+{
+    if (!h || bytes < 0 || (buf != nullptr && (reinterpret_cast<uintptr_t>(buf) % 8) != 0))
+        return fail(TL_ERR_INVALID_ARG, "bad argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->trace = (buf != nullptr && bytes > 0) ? static_cast<unsigned long long*>(buf) : nullptr;
+    h->trace_bytes = h->trace ? bytes : 0;
     return TL_SUCCESS;
 }
 

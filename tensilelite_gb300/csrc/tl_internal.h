@@ -101,6 +101,8 @@ struct TcLaunch {
     int epi_act;
     int epi_on;
     int debug_flags;         // tl_gemm_solution.debug_flags (TL_DEBUG_SKIP_LOADS)
+    unsigned long long* trace;   // device timeline (tl_set_trace) or null
+    int64_t trace_bytes;
 };
 
 // Dynamic shared memory of one CTA staging bm_cta m-rows per stage (bm / 2 for a CTA pair).

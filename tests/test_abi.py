@@ -104,6 +104,21 @@ def test_status_strings_and_errors():
     assert b"NULL" in L.tl_last_error_string()
 
 
+def test_trace_argument_checks():
+    """tl_set_trace needs a handle and an 8-byte aligned buffer; NULL switches it off (no GPU use)."""
+    L = tl.lib()
+    assert tl.TRACE_SLOTS == 16 and len(tl.TRACE_EVENTS) == tl.TRACE_SLOTS
+    assert L.tl_set_trace(None, None, 0) == tl.ERR_INVALID_ARG
+    h = ctypes.c_void_p()
+    tl.check(L.tl_init_host(152, 232448, 0, ctypes.byref(h)))
+    try:
+        assert L.tl_set_trace(h, ctypes.c_void_p(0x1004), 4096) == tl.ERR_INVALID_ARG
+        assert L.tl_set_trace(h, ctypes.c_void_p(0x1000), -8) == tl.ERR_INVALID_ARG
+        tl.check(L.tl_set_trace(h, None, 0))
+    finally:
+        tl.check(L.tl_destroy(h))
+
+
 @pytest.mark.parametrize("rounding", [tl.ROUND_RNE, tl.ROUND_TRUNCATE])
 def test_host_convert_bf16(rounding):
     conv = np.load(os.path.join(ROOT, "tests", "golden", "converters.npz"))
