@@ -435,6 +435,10 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
                        ? 1
                        : 0;
     kp.direct_last = last_direct_enabled() ? 1 : 0;
+    kp.narrow = (kp.total_work < (int64_t(1) << 31) && tiles < (int64_t(1) << 31) &&
+                 static_cast<int64_t>(kp.num_kb) * (kp.tail_split + 1) < (int64_t(1) << 31))
+                    ? 1
+                    : 0;
     kp.ws = L.workspace;
     kp.counters = L.counters;
     kp.err = L.err;

@@ -48,6 +48,7 @@ struct TcKernelParams {
     int promote_kb;               // >0: the A0*B0 product restarts its TMEM chain every promote_kb
                                   // k-blocks; the epilogue adds each chain into fp32 registers
     int tiles_m, tiles_n;
+    int narrow;                   // work units, tiles and split k-block products fit 32 bits
     int64_t total_work;
     int64_t split_units;          // work units below this are k-slices of the first split_tiles tiles
     int64_t split_tiles;          // tiles split along k; the rest are whole
@@ -150,11 +151,20 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, cons
             }
         } else if (w < p.split_units) {
             // split tiles come first, so the last arriver's reduction overlaps later whole tiles
-            tile = w / p.tail_split;
-            split = static_cast<int>(w % p.tail_split);
             nsplit = p.tail_split;
-            kb0 = static_cast<int>((static_cast<int64_t>(split) * p.num_kb) / nsplit);
-            kb1 = static_cast<int>((static_cast<int64_t>(split + 1) * p.num_kb) / nsplit);
+            if (p.narrow) {
+                const uint32_t uw = static_cast<uint32_t>(w), ts = static_cast<uint32_t>(nsplit);
+                const uint32_t q = uw / ts, nkb = static_cast<uint32_t>(p.num_kb);
+                tile = q;
+                split = static_cast<int>(uw - q * ts);
+                kb0 = static_cast<int>((static_cast<uint32_t>(split) * nkb) / ts);
+                kb1 = static_cast<int>((static_cast<uint32_t>(split + 1) * nkb) / ts);
+            } else {
+                tile = w / p.tail_split;
+                split = static_cast<int>(w % p.tail_split);
+                kb0 = static_cast<int>((static_cast<int64_t>(split) * p.num_kb) / nsplit);
+                kb1 = static_cast<int>((static_cast<int64_t>(split + 1) * p.num_kb) / nsplit);
+            }
         } else {
             tile = p.split_tiles + (w - p.split_units);
             split = 0;
@@ -162,21 +172,45 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, cons
             kb0 = 0;
             kb1 = p.num_kb;
         }
-        const int64_t tpb = static_cast<int64_t>(p.tiles_m) * p.tiles_n;
-        const int b = static_cast<int>(tile / tpb);
-        const int64_t t = tile % tpb;
-        int in, jm;
-        if (p.raster > 0) {
-            const int64_t group_tiles = static_cast<int64_t>(p.raster) * p.tiles_m;
-            const int64_t g = t / group_tiles;
-            const int first_n = static_cast<int>(g * p.raster);
-            const int gsize = min(p.raster, p.tiles_n - first_n);
-            const int64_t r = t % group_tiles;
-            in = first_n + static_cast<int>(r % gsize);
-            jm = static_cast<int>(r / gsize);
+        int b, in, jm;
+        if (p.narrow) {
+            // every tile index fits 32 bits (host-checked): 32-bit divisions are several times
+            // shorter than 64-bit ones, and this decode sits between the launch and the first load
+            const uint32_t ut = static_cast<uint32_t>(tile);
+            const uint32_t tpb = static_cast<uint32_t>(p.tiles_m) * static_cast<uint32_t>(p.tiles_n);
+            const uint32_t ub = ut / tpb;
+            const uint32_t t = ut - ub * tpb;
+            b = static_cast<int>(ub);
+            if (p.raster > 0) {
+                const uint32_t group_tiles = static_cast<uint32_t>(p.raster) * static_cast<uint32_t>(p.tiles_m);
+                const uint32_t g = t / group_tiles;
+                const int first_n = static_cast<int>(g * static_cast<uint32_t>(p.raster));
+                const uint32_t gsize = static_cast<uint32_t>(min(p.raster, p.tiles_n - first_n));
+                const uint32_t r = t - g * group_tiles;
+                const uint32_t rq = r / gsize;
+                in = first_n + static_cast<int>(r - rq * gsize);
+                jm = static_cast<int>(rq);
+            } else {
+                const uint32_t q = t / static_cast<uint32_t>(p.tiles_m);
+                in = static_cast<int>(q);
+                jm = static_cast<int>(t - q * static_cast<uint32_t>(p.tiles_m));
+            }
         } else {
-            in = static_cast<int>(t / p.tiles_m);
-            jm = static_cast<int>(t % p.tiles_m);
+            const int64_t tpb = static_cast<int64_t>(p.tiles_m) * p.tiles_n;
+            b = static_cast<int>(tile / tpb);
+            const int64_t t = tile % tpb;
+            if (p.raster > 0) {
+                const int64_t group_tiles = static_cast<int64_t>(p.raster) * p.tiles_m;
+                const int64_t g = t / group_tiles;
+                const int first_n = static_cast<int>(g * p.raster);
+                const int gsize = min(p.raster, p.tiles_n - first_n);
+                const int64_t r = t % group_tiles;
+                in = first_n + static_cast<int>(r % gsize);
+                jm = static_cast<int>(r / gsize);
+            } else {
+                in = static_cast<int>(t / p.tiles_m);
+                jm = static_cast<int>(t % p.tiles_m);
+            }
         }
         j.tmN = &p.tmN[0];
         j.tmM = &p.tmM[0];
@@ -718,7 +752,7 @@ __device__ __forceinline__ void split_finish_parallel(const TcKernelParams& p, f
                                                       int et,
                                                       int lane, int row, bool row_ok, int64_t base_c, int64_t base_d,
                                                       volatile int* last_flag, uint64_t* tempty_bar,
-                                                      volatile int* abort_flag)
+                                                      volatile int* abort_flag, bool c_staged, uint32_t c_row)
 {
     if (ok) release_tmem<CG>(tempty_bar, lane);     // this split's partial is in the workspace
     __threadfence();
@@ -740,26 +774,59 @@ __device__ __forceinline__ void split_finish_parallel(const TcKernelParams& p, f
         const size_t slab_elems = static_cast<size_t>(kTcTileN) * p.bm;
         const float* base = p.ws + static_cast<size_t>(j.slot) * p.tail_split * slab_elems + row;
         for (int c = j.split; c < chunks; c += j.nsplit) {
+            const int m = j.m0 + c * 32;
+            const bool live = row_ok && m < j.M;
+            // two splits' partials at a time are in flight together (the reduction is
+            // latency-bound), summed in split order
             float v[32];
 #pragma unroll
             for (int i = 0; i < 32; ++i) v[i] = 0.f;
-            for (int s = 0; s < j.nsplit; ++s) {
-                float a[32];
-                const float* src = base + static_cast<size_t>(s) * slab_elems + static_cast<size_t>(c) * 32 * kTcTileN;
+            for (int s = 0; s < j.nsplit; s += 2) {
+                float a[32], b[32];
+                const float* sa = base + static_cast<size_t>(s) * slab_elems + static_cast<size_t>(c) * 32 * kTcTileN;
+                const bool two = s + 1 < j.nsplit;
 #pragma unroll
-                for (int i = 0; i < 32; ++i) a[i] = __ldcg(src + i * kTcTileN);
+                for (int i = 0; i < 32; ++i) {
+                    a[i] = __ldcg(sa + i * kTcTileN);
+                    b[i] = two ? __ldcg(sa + slab_elems + i * kTcTileN) : 0.f;
+                }
 #pragma unroll
                 for (int i = 0; i < 32; ++i) v[i] += a[i];
+                if (two) {
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) v[i] += b[i];
+                }
             }
-            const int m = j.m0 + c * 32;
-            if (row_ok && m < j.M) store_chunk<TD, EPI>(p, amax, j, base_c, base_d, m, v, p.out_trunc);
+            if (live) {
+                if (c == j.split && c_staged) {
+                    // this chunk's C row was copied into shared memory while the tile accumulated
+                    // (16-byte unit u at u ^ (lane & 7))
+                    uint32_t cw[32];
+                    ptx::cp_async_wait0();
+                    constexpr int NU = 32 * static_cast<int>(sizeof(TD)) / 16;
+#pragma unroll
+                    for (int u = 0; u < NU; ++u) {
+                        const uint4 w4 = ptx::ld_shared_v4(c_row + static_cast<uint32_t>((u ^ (lane & 7)) * 16));
+                        cw[4 * u] = w4.x;
+                        cw[4 * u + 1] = w4.y;
+                        cw[4 * u + 2] = w4.z;
+                        cw[4 * u + 3] = w4.w;
+                    }
+                    store_chunk_pre<TD, EPI>(p, amax, j, base_d, m, v, cw, p.out_trunc);
+                } else {
+                    store_chunk<TD, EPI>(p, amax, j, base_c, base_d, m, v, p.out_trunc);
+                }
+            }
         }
     } else {
         ok = false;
     }
+    if (c_staged) ptx::cp_async_wait0();   // the staging buffer is free again (also on the error path)
     asm volatile("bar.sync 1, 128;" ::: "memory");
     if (et == 0 && go) {
-        __threadfence();
+        // counts this split out of the tile: the last one resets the counter for the next launch.
+        // No fence: the counter only orders the splits' waits (same-address atomics), and the next
+        // launch's use of the workspace is ordered by the kernel boundary.
         if (atomicAdd(p.counters + j.slot, 1) == 2 * j.nsplit - 1) atomicExch(p.counters + j.slot, 0);
     }
     asm volatile("bar.sync 1, 128;" ::: "memory");   // last_flag is reused by the next tile
@@ -856,6 +923,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
     ptx::tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
     if (threadIdx.x == 0) trace_mark(p, TL_TRACE_SETUP);
+    // The first work unit's job depends only on the launch parameters: decode it while the
+    // previous grid in the stream may still be running.
+    TileJob job0;
+    if (p.group == nullptr && unit0 < p.total_work) get_job(p, unit0, make_int4(0, 0, 0, 0), job0);
     // Launched as a programmatic dependent: everything above (barrier set-up, TMEM allocation,
     // descriptor prefetch) may have run while the previous kernel in the stream was finishing.
     // Wait for that grid to complete (its writes visible) before touching global memory, then let
@@ -882,7 +953,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 const int4 u = u_next;
                 u_next = load_unit(p, w + units);      // in flight during this tile
                 TileJob j;
-                get_job(p, w, u, j);
+                if (w == unit0 && p.group == nullptr) j = job0;
+                else get_job(p, w, u, j);
                 const int n0 = j.n0 + static_cast<int>(rank) * kTcTileN;
                 const int m0 = j.m0 + static_cast<int>(pair_rank * bmc);
                 const int total = (j.kb1 - j.kb0) * nvirt;
@@ -989,7 +1061,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 const int4 u = u_next;
                 u_next = load_unit(p, w + units);      // in flight during this tile
                 TileJob j;
-                get_job(p, w, u, j);
+                if (w == unit0 && p.group == nullptr) j = job0;
+                else get_job(p, w, u, j);
                 const int nkb = j.kb1 - j.kb0;
                 if (nkb <= 0) continue;                 // an empty unit of a balanced split
                 const int chunk = promo ? p.promote_kb : nkb;
@@ -1213,6 +1286,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 continue;
             }
             // ---- one TMEM accumulator per tile
+            // parallel split-k: this split finishes 32-column chunk `split` of the tile.  Its C does
+            // not depend on the accumulator: each thread copies its row of it into the warp's
+            // output staging buffer (free in this mode: no TMA store is in flight from it) while the
+            // tile accumulates.
+            bool c_staged = false;
+            const uint32_t c_row = ptx::smem_u32(epi_stage) + static_cast<uint32_t>(quarter) * 4096u +
+                                   static_cast<uint32_t>(lane) * 128u;
+            if constexpr (sizeof(TD) >= 2) {
+                const int mc = j.m0 + j.split * 32;
+                if (p.par_reduce && j.nsplit > 1 && j.beta != 0.0f && j.C != nullptr && j.split * 32 < p.bm) {
+                    if (lane == 0) ptx::bulk_wait_read0();
+                    __syncwarp();
+                    const char* cptr = static_cast<const char*>(j.C) + (base_c + mc) * static_cast<int64_t>(sizeof(TD));
+                    if (row_ok && mc + 32 <= j.M && (reinterpret_cast<uintptr_t>(cptr) & 15) == 0) {
+                        constexpr int NU = 32 * static_cast<int>(sizeof(TD)) / 16;
+#pragma unroll
+                        for (int u = 0; u < NU; ++u)
+                            ptx::cp_async16(c_row + static_cast<uint32_t>((u ^ (lane & 7)) * 16), cptr + 16 * u);
+                        c_staged = true;
+                    }
+                    ptx::cp_async_commit();
+                }
+            }
             bool got = ok && ptx::mbar_wait(&tfull[mbuf], mph, tlim, abort_flag);
             got = __all_sync(0xffffffffu, got);
             if (ok && !got) {
@@ -1296,7 +1392,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 if (tr) trace_mark(p, TL_TRACE_STORED);
                 if (p.par_reduce)
                     split_finish_parallel<TD, CG, EPI>(p, amax, j, ok, et, lane, row, row_ok, base_c, base_d, last_flag,
-                                                  &tempty[mbuf], abort_flag);
+                                                  &tempty[mbuf], abort_flag, c_staged, c_row);
                 else
                     split_finish_tmem<TD, CG, EPI>(p, amax, j, ok, et, lane, row, row_ok, base_c, base_d, last_flag, tbase,
                                               &tempty[mbuf]);
