@@ -305,6 +305,9 @@ double tc_cost(const tl_handle* h, const tl_gemm_problem& p, const tl_gemm_solut
         const double part = static_cast<double>(kTcTileN) * bm * 4.0 / 27.0;
         if (units <= workers) cost += 1500.0 + part + (part * split + epi) / split;
         else cost += 3000.0 + part + part * split + epi;
+        // a CTA pair's split epilogue (remote TMEM hand-backs, both CTAs parking) measured ~0.7 us
+        // longer than one CTA's on bf16 480 x 1024 x 4096 at split-k 4
+        if (cg >= 2) cost += 1400.0;
     }
     return cost;
 }

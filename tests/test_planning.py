@@ -72,9 +72,9 @@ DEVICE_PICKS = [
     ("bf16 dX 1024x4096x4096 TN", dict(m=1024, n=4096, k=4096, trans_a=True), (256, 512, 1, 6, 0, 0, 64)),
     ("bf16 dW 4096x1024x4096 NT", dict(m=4096, n=1024, k=4096, trans_b=True), (256, 512, 1, 6, 0, 0, 64)),
     ("bf16 1024x4096x4096 NN", dict(m=1024, n=4096, k=4096), (256, 512, 1, 6, 0, 0, 64)),
-    ("bf16 480x1024x4096 NN", dict(m=480, n=1024, k=4096), (128, 256, 4, 6, 0, 0, 64)),
+    ("bf16 480x1024x4096 NN", dict(m=480, n=1024, k=4096), (128, 128, 4, 6, 0, 0, 64)),
     ("bf16 1024^3 NN", dict(m=1024, n=1024, k=1024), (128, 256, 1, 6, 0, 0, 64)),
-    ("bf16 1024x1024x4096 NN", dict(m=1024, n=1024, k=4096), (128, 256, 2, 6, 0, 0, 64)),
+    ("bf16 1024x1024x4096 NN", dict(m=1024, n=1024, k=4096), (192, 128, 3, 5, 0, 0, 64)),
     ("fp8 8192^3 TN", dict(m=8192, n=8192, k=8192, dtype="fp8", trans_a=True), (256, 512, 1, 6, 8, 0, 128)),
     ("bf16x6 8192^3 NN", dict(m=8192, n=8192, k=8192, dtype="fp32", kernel="bf16x6"), (128, 256, 1, 6, 8, 256, 64)),
 ]
