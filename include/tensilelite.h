@@ -415,7 +415,7 @@ enum {
     TL_TRACE_ENTRY_NS = 1,     /* %globaltimer at entry */
     TL_TRACE_SETUP = 2,        /* barriers initialised, TMEM allocated, CTAs of the cluster in step */
     TL_TRACE_DEP = 3,          /* the previous grid in the stream has completed (programmatic launch) */
-    TL_TRACE_LOAD_FIRST = 4,   /* producer: first tile's first TMA load issued */
+    TL_TRACE_LOAD_FIRST = 4,   /* producer: starts issuing the first tile's TMA loads */
     TL_TRACE_LOAD_LAST = 5,    /* producer: first tile's last TMA load issued */
     TL_TRACE_MMA_FIRST = 6,    /* MMA warp: first tile's first stage landed */
     TL_TRACE_MMA_LAST = 7,     /* MMA warp: first tile's last MMA committed */

@@ -923,10 +923,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
     ptx::tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
     if (threadIdx.x == 0) trace_mark(p, TL_TRACE_SETUP);
-    // The first work unit's job depends only on the launch parameters: decode it while the
-    // previous grid in the stream may still be running.
-    TileJob job0;
-    if (p.group == nullptr && unit0 < p.total_work) get_job(p, unit0, make_int4(0, 0, 0, 0), job0);
     // Launched as a programmatic dependent: everything above (barrier set-up, TMEM allocation,
     // descriptor prefetch) may have run while the previous kernel in the stream was finishing.
     // Wait for that grid to complete (its writes visible) before touching global memory, then let
@@ -953,12 +949,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 const int4 u = u_next;
                 u_next = load_unit(p, w + units);      // in flight during this tile
                 TileJob j;
-                if (w == unit0 && p.group == nullptr) j = job0;
-                else get_job(p, w, u, j);
+                get_job(p, w, u, j);
                 const int n0 = j.n0 + static_cast<int>(rank) * kTcTileN;
                 const int m0 = j.m0 + static_cast<int>(pair_rank * bmc);
                 const int total = (j.kb1 - j.kb0) * nvirt;
                 int kb = j.kb0, v = 0;
+                // timeline stamps stay outside the k-block loops (a branch there slows the issue)
+                if (w == unit0 && lane == 0) trace_mark(p, TL_TRACE_LOAD_FIRST);
                 for (int i = 0; i < total; ++i) {
                     if (!__all_sync(0xffffffffu, ptx::mbar_wait(&empty[stage], phase ^ 1u, tlim))) {
                         if (lane == 0) record_error(p, abort_flag, 1);
@@ -1026,8 +1023,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         }
                     }
                     __syncwarp();
-                    if (w == unit0 && lane == 0 && (i == 0 || i == total - 1))
-                        trace_mark(p, i == 0 ? TL_TRACE_LOAD_FIRST : TL_TRACE_LOAD_LAST);
                     if (++stage == static_cast<uint32_t>(nstages)) {
                         stage = 0;
                         phase ^= 1u;
@@ -1037,6 +1032,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         ++kb;
                     }
                 }
+                if (w == unit0 && lane == 0) trace_mark(p, TL_TRACE_LOAD_LAST);
             }
         }
     } else if (warp == 1) {
@@ -1061,8 +1057,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 const int4 u = u_next;
                 u_next = load_unit(p, w + units);      // in flight during this tile
                 TileJob j;
-                if (w == unit0 && p.group == nullptr) j = job0;
-                else get_job(p, w, u, j);
+                get_job(p, w, u, j);
                 const int nkb = j.kb1 - j.kb0;
                 if (nkb <= 0) continue;                 // an empty unit of a balanced split
                 const int chunk = promo ? p.promote_kb : nkb;
@@ -1083,6 +1078,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                 bool main_started = false, small_started = false;
                 const int total = nkb * nvirt;
                 int v = 0, kb_in_chain = 0;
+                if (p.trace != nullptr && w == unit0 && total > 0) {
+                    // timeline: the first stage's arrival, waited for here (the loop's own wait on
+                    // it then passes at once) so that the k-block loop carries no stamp
+                    ptx::mbar_wait(&full[stage], phase, tlim);
+                    if (lane == 0) trace_mark(p, TL_TRACE_MMA_FIRST);
+                    __syncwarp();
+                }
                 for (int i = 0; i < total; ++i) {
                     if (!__all_sync(0xffffffffu, ptx::mbar_wait(&full[stage], phase, tlim))) {
                         if (lane == 0) record_error(p, abort_flag, 4);
@@ -1090,7 +1092,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                         break;
                     }
                     ptx::tc_fence_after();
-                    if (i == 0 && w == unit0 && lane == 0) trace_mark(p, TL_TRACE_MMA_FIRST);
                     const bool is_main = !sep_small || v == nvirt - 1;
                     const uint32_t d_tmem = tmem_base + (is_main ? mbuf * bmu : (2u + sbuf) * bmu);
                     const bool started = is_main ? main_started : small_started;
