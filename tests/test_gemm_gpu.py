@@ -196,6 +196,24 @@ def test_split_k_reductions(h, cg, bm, split):
         check_case(h, case, "bf16", kernel="tcgen05", solution=sol)
 
 
+@pytest.mark.parametrize("od", ["bf16", "fp16", "fp32"])
+@pytest.mark.parametrize("m", [480, 479])
+def test_parallel_split_k_c_staging(h, od, m):
+    """Parallel split-k with beta: a split copies the C rows of the chunk it finishes into shared
+    memory while the tile accumulates, when the row segment is whole and 16-byte aligned, else it
+    reads C at the end.  m = 479 (odd leading dimension of C and D, ragged last m-tile) mixes both
+    in one launch; every output type."""
+    dt = "fp16" if od == "fp16" else "bf16"
+    case = gg.make_case(dt, "NN", 1300 + m, m, 1024, 2048, alpha=1.25, beta=0.5, ld_align=8)
+    sol = tl.Solution(kernel=tl.KERNEL_TCGEN05, macro_tile0=128, macro_tile1=128, depth_u=64, stages=4,
+                      split_k=4)
+    got = gu.run_case(h, case, kernel="tcgen05", dtype=dt, out_dtype=od, solution=sol)
+    n, k = case["n"], case["k"]
+    G = gu.mat(got, m, n, case["ldc"])
+    R = gu.mat(gu.oracle_ref(case), m, n, m)
+    assert_close(G, R, absprod_of(case), k, case["alpha"], case["beta"], gu.mat(case["C"], m, n, case["ldc"]), od)
+
+
 @pytest.mark.parametrize("cg,bm", [(1, 256), (2, 256), (4, 256), (2, 128)])
 @pytest.mark.parametrize("m,n,k", [(256, 512, 8192), (1000, 3008, 1344), (2048, 4608, 576)])
 def test_balanced_split_shapes(h, cg, bm, m, n, k):
