@@ -299,6 +299,30 @@ bool tc_encode_output(CUtensorMap* tm, int out_dtype, void* D, int64_t M, int64_
                CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// The caller's D for a transposed output: the kernel's n runs along D's rows (dimension 0, N of
+// the launch) and its m along D's columns; boxes of 32 x 32 elements, one epilogue warp's rows by
+// one 32-column chunk, unswizzled (a 64- or 128-byte inner extent).
+bool tc_encode_output_t(CUtensorMap* tm, int out_dtype, void* D, int64_t rows, int64_t cols, int64_t ldd,
+                        int64_t batch, int64_t stride_d)
+{
+    EncodeTiledFn enc = get_encode_fn();
+    if (!enc || !D) return false;
+    if (out_dtype != TL_DTYPE_FP32 && out_dtype != TL_DTYPE_FP16 && out_dtype != TL_DTYPE_BF16) return false;
+    const int es = dtype_bytes(out_dtype);
+    if ((reinterpret_cast<uintptr_t>(D) & 15) || (ldd * es) % 16 || (batch > 1 && (stride_d * es) % 16)) return false;
+    const CUtensorMapDataType dt = out_dtype == TL_DTYPE_FP32   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                   : out_dtype == TL_DTYPE_FP16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                                : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    cuuint64_t dims[3] = {static_cast<cuuint64_t>(rows), static_cast<cuuint64_t>(cols), static_cast<cuuint64_t>(batch)};
+    cuuint64_t strides[2] = {static_cast<cuuint64_t>(ldd) * es,
+                             batch > 1 ? static_cast<cuuint64_t>(stride_d) * es
+                                       : ((static_cast<cuuint64_t>(ldd) * es * cols) + 15) & ~cuuint64_t(15)};
+    cuuint32_t box[3] = {32, 32, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    return enc(tm, dt, 3, D, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launches)
 {
     TcKernelParams kp;
@@ -430,10 +454,17 @@ tl_status tc_gemm_launch(const TcLaunch& L, cudaStream_t stream, int64_t* launch
     }
     // whole tiles leave through TMA stores (not with promotion, which drains chains into registers)
     // (an fp8 output's 128-byte box is 128 columns wide: only tiles made of whole boxes)
-    kp.tma_store = (L.promote_k == 0 && tma_store_enabled() && (L.out_dtype != TL_DTYPE_FP8_E4M3 || L.bm % 128 == 0) &&
-                    tc_encode_output(&kp.tmD, L.out_dtype, L.D, L.M, L.N, L.ldd, L.batch, L.stride_d))
-                       ? 1
-                       : 0;
+    kp.out_t = L.out_t;
+    if (L.out_t)
+        kp.tma_store = (L.promote_k == 0 && tma_store_enabled() &&
+                        tc_encode_output_t(&kp.tmD, L.out_dtype, L.D, L.N, L.M, L.ldd, L.batch, L.stride_d))
+                           ? 1
+                           : 0;
+    else
+        kp.tma_store = (L.promote_k == 0 && tma_store_enabled() && (L.out_dtype != TL_DTYPE_FP8_E4M3 || L.bm % 128 == 0) &&
+                        tc_encode_output(&kp.tmD, L.out_dtype, L.D, L.M, L.N, L.ldd, L.batch, L.stride_d))
+                           ? 1
+                           : 0;
     kp.direct_last = last_direct_enabled() ? 1 : 0;
     kp.narrow = (kp.total_work < (int64_t(1) << 31) && tiles < (int64_t(1) << 31) &&
                  static_cast<int64_t>(kp.num_kb) * (kp.tail_split + 1) < (int64_t(1) << 31))

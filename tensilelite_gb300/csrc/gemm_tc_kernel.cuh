@@ -71,6 +71,8 @@ struct TcKernelParams {
     unsigned long long timeout_ns;
     int debug_skip_loads;         // TL_DEBUG_SKIP_LOADS: the producer issues no copies (timeout-path test)
     unsigned long long* trace;    // device timeline, TL_TRACE_SLOTS words per CTA, or null
+    int out_t;                    // D and C are the transpose of the kernel's output: element (m, n)
+                                  // at n + m * ld (an NN problem run as its transposed TT product)
 };
 
 // Timeline stamp of event `slot` for this CTA (tl_set_trace): the SM cycle counter.
@@ -105,6 +107,7 @@ struct TileJob {
     int b, n0, m0;
     int kb0, kb1;
     int split, nsplit;            // this unit's k split and the tile's number of splits
+    int out_t;                    // transposed output (TcKernelParams::out_t)
     int64_t tile;
     int64_t slot;                 // split tiles: index of the tile's workspace slabs and counter
 };
@@ -230,6 +233,7 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, cons
         j.kb1 = kb1;
         j.split = split;
         j.nsplit = nsplit;
+        j.out_t = p.out_t;
         j.tile = tile;
         j.slot = tile;                 // split tiles are 0 .. split_tiles-1
     } else {
@@ -254,6 +258,7 @@ __device__ __forceinline__ void get_job(const TcKernelParams& p, int64_t w, cons
         j.kb1 = u.w;
         j.split = 0;
         j.nsplit = 1;
+        j.out_t = 0;
         j.tile = w;
         j.slot = 0;
     }
@@ -374,7 +379,7 @@ __device__ __forceinline__ void store_chunk(const TcKernelParams& p, float& amax
     const bool use_c = (j.beta != 0.0f) && (j.C != nullptr);
     char* dptr = static_cast<char*>(j.D) + (base_d + m) * Out<TD>::kBytes;
     const char* cptr = use_c ? static_cast<const char*>(j.C) + (base_c + m) * Out<TD>::kBytes : nullptr;
-    const bool vec = full && ((reinterpret_cast<uintptr_t>(dptr) & 15) == 0) &&
+    const bool vec = full && !j.out_t && ((reinterpret_cast<uintptr_t>(dptr) & 15) == 0) &&
                      (!use_c || (reinterpret_cast<uintptr_t>(cptr) & 15) == 0);
     if (vec) {
         if constexpr (sizeof(TD) == 4) {
@@ -443,14 +448,25 @@ __device__ __forceinline__ void store_chunk(const TcKernelParams& p, float& amax
             }
         }
     } else {
+        // element m + i at (m + i) * step: 1, or ld for a transposed output (a warp's 32 rows then
+        // make one coalesced access per element)
+        // C in groups of sixteen, each group read before its D is written: the loads of a group
+        // overlap (a store may alias a later load, so none is moved above one), and D may be C itself
+        const int64_t dstep = j.out_t ? j.ldd : 1, cstep = j.out_t ? j.ldc : 1;
 #pragma unroll
-        for (int i = 0; i < 32; ++i) {
-            if (m + i < j.M) {
-                float o;
-                if (use_c) o = fmaf(j.alpha, acc[i], j.beta * Out<TD>::load(j.C, base_c + m + i));
-                else o = j.alpha * acc[i];
-                if constexpr (EPI) o = epi_fn(p, m + i, true, o, amax);
-                Out<TD>::store(j.D, base_d + m + i, out_scale<TD>(p, o), trunc);
+        for (int i0 = 0; i0 < 32; i0 += 16) {
+            float cv[16];
+#pragma unroll
+            for (int t = 0; t < 16; ++t)
+                cv[t] = (use_c && m + i0 + t < j.M) ? Out<TD>::load(j.C, base_c + (m + i0 + t) * cstep) : 0.f;
+#pragma unroll
+            for (int t = 0; t < 16; ++t) {
+                const int i = i0 + t;
+                if (m + i < j.M) {
+                    float o = use_c ? fmaf(j.alpha, acc[i], j.beta * cv[t]) : j.alpha * acc[i];
+                    if constexpr (EPI) o = epi_fn(p, m + i, true, o, amax);
+                    Out<TD>::store(j.D, base_d + (m + i) * dstep, out_scale<TD>(p, o), trunc);
+                }
             }
         }
     }
@@ -517,7 +533,7 @@ __device__ __forceinline__ void load_c_chunk(const TileJob& j, int64_t base_c, i
     if constexpr (sizeof(TD) == 1) return;        // fp8 outputs take beta == 0: no C
     if (!(j.beta != 0.0f && j.C != nullptr) || m >= j.M) return;
     const char* cptr = static_cast<const char*>(j.C) + (base_c + m) * Out<TD>::kBytes;
-    if (m + 32 <= j.M && (reinterpret_cast<uintptr_t>(cptr) & 15) == 0) {
+    if (!j.out_t && m + 32 <= j.M && (reinterpret_cast<uintptr_t>(cptr) & 15) == 0) {
         constexpr int nvec = sizeof(TD) == 4 ? 8 : 4;
 #pragma unroll
         for (int q = 0; q < nvec; ++q) {
@@ -529,8 +545,9 @@ __device__ __forceinline__ void load_c_chunk(const TileJob& j, int64_t base_c, i
         }
     } else {
 #pragma unroll
+        const int64_t cstep = j.out_t ? j.ldc : 1;
         for (int i = 0; i < 32; ++i) {
-            const float c = (m + i < j.M) ? Out<TD>::load(j.C, base_c + m + i) : 0.f;
+            const float c = (m + i < j.M) ? Out<TD>::load(j.C, base_c + (m + i) * cstep) : 0.f;
             if constexpr (sizeof(TD) == 4) {
                 cw[i] = __float_as_uint(c);
             } else {
@@ -619,7 +636,7 @@ __device__ __forceinline__ void store_chunk_pre(const TcKernelParams& p, float& 
         for (int i = 0; i < 32; ++i) o[i] = epi_fn(p, m + i, m + i < j.M, o[i], amax);
     }
     char* dptr = static_cast<char*>(j.D) + (base_d + m) * Out<TD>::kBytes;
-    if (m + 32 <= j.M && (reinterpret_cast<uintptr_t>(dptr) & 15) == 0) {
+    if (!j.out_t && m + 32 <= j.M && (reinterpret_cast<uintptr_t>(dptr) & 15) == 0) {
         if constexpr (sizeof(TD) == 4) {
 #pragma unroll
             for (int q = 0; q < 8; ++q)
@@ -634,9 +651,10 @@ __device__ __forceinline__ void store_chunk_pre(const TcKernelParams& p, float& 
                                pack2(o[8 * q + 6], o[8 * q + 7], is_half, trunc));
         }
     } else {
+        const int64_t dstep = j.out_t ? j.ldd : 1;
 #pragma unroll
         for (int i = 0; i < 32; ++i)
-            if (m + i < j.M) Out<TD>::store(j.D, base_d + m + i, o[i], trunc);
+            if (m + i < j.M) Out<TD>::store(j.D, base_d + (m + i) * dstep, o[i], trunc);
     }
 }
 
@@ -1193,15 +1211,34 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             j.slot = j.slot * CL + rank;              // split-k slabs and counters per CTA
             const int n = j.n0 + row;
             const bool row_ok = n < j.N;
-            const int64_t base_d = static_cast<int64_t>(j.b) * p.stride_d + static_cast<int64_t>(n) * j.ldd;
-            const int64_t base_c = static_cast<int64_t>(j.b) * p.stride_c + static_cast<int64_t>(n) * j.ldc;
-            if (ok && row_ok && j.beta != 0.0f && j.C != nullptr && (j.nsplit == 1 || j.split == j.nsplit - 1)) {
+            // this thread's row n of the output: a contiguous run of m, or with a transposed output
+            // one element of each of the columns m (stride ld)
+            const int64_t base_d = static_cast<int64_t>(j.b) * p.stride_d + static_cast<int64_t>(n) * (j.out_t ? 1 : j.ldd);
+            const int64_t base_c = static_cast<int64_t>(j.b) * p.stride_c + static_cast<int64_t>(n) * (j.out_t ? 1 : j.ldc);
+            if (ok && row_ok && !j.out_t && j.beta != 0.0f && j.C != nullptr && (j.nsplit == 1 || j.split == j.nsplit - 1)) {
                 // C does not depend on the accumulator: start pulling this row's segment into L2
                 // while the tile is still accumulating
                 const char* cp = static_cast<const char*>(j.C) + (base_c + j.m0) * static_cast<int64_t>(sizeof(TD));
                 const int cbytes = (min(p.bm, j.M - j.m0)) * static_cast<int>(sizeof(TD));
                 for (int off = 0; off < cbytes; off += 128)
                     asm volatile("prefetch.global.L2 [%0];" ::"l"(cp + off));
+            }
+            if (ok && j.out_t && j.beta != 0.0f && j.C != nullptr) {
+                // transposed output: the warp's C is a 64- or 128-byte run of each column; lane L
+                // pulls column L of every 32-column chunk into L2 (both lines a run may touch)
+                const int nrow0 = j.n0 + quarter * 32;
+                if (nrow0 < j.N) {
+                    for (int c = 0; c < chunks; ++c) {
+                        const int ccol = j.m0 + c * 32 + lane;
+                        if (ccol >= j.M) break;
+                        const char* cp = static_cast<const char*>(j.C) +
+                                         (static_cast<int64_t>(j.b) * p.stride_c + static_cast<int64_t>(ccol) * j.ldc + nrow0) *
+                                             static_cast<int64_t>(sizeof(TD));
+                        const int last = (min(32, j.N - nrow0) * static_cast<int>(sizeof(TD))) - 1;
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(cp));
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(cp + last));
+                    }
+                }
             }
             if (promo) {
                 // ---- promotion: sum the A0*B0 chains (and the small terms) in fp32 registers; bm == 128
@@ -1296,7 +1333,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
                                    static_cast<uint32_t>(lane) * 128u;
             if constexpr (sizeof(TD) >= 2) {
                 const int mc = j.m0 + j.split * 32;
-                if (p.par_reduce && j.nsplit > 1 && j.beta != 0.0f && j.C != nullptr && j.split * 32 < p.bm) {
+                if (p.par_reduce && !j.out_t && j.nsplit > 1 && j.beta != 0.0f && j.C != nullptr && j.split * 32 < p.bm) {
                     if (lane == 0) ptx::bulk_wait_read0();
                     __syncwarp();
                     const char* cptr = static_cast<const char*>(j.C) + (base_c + mc) * static_cast<int64_t>(sizeof(TD));
@@ -1323,7 +1360,99 @@ __global__ void __launch_bounds__(kTcThreads, 1) tc_gemm_kernel(const __grid_con
             // refilled only after the previous store has read it): hidden behind the next tile's
             // main loop, but exposed on a CTA's last tile, which uses the direct stores instead
             // when beta == 0 (with a C operand to read, the staged path measured faster).
-            const bool direct = p.direct_last && j.beta == 0.0f && w + units >= p.total_work;
+            const bool direct = p.direct_last && !j.out_t && j.beta == 0.0f && w + units >= p.total_work;
+            if constexpr (sizeof(TD) >= 2 && !EPI) {
+                if (j.out_t && j.nsplit == 1 && j.tmD != nullptr) {
+                    // transposed output: a warp's 32 rows are 32 consecutive elements of D's columns,
+                    // so each 32-column chunk is one 32 x 32 box of D, staged [column][row] (two boxes
+                    // per 4 KB buffer for 16-bit outputs, one for fp32) and written by one TMA store;
+                    // a box's buffer is refilled once the store two (16-bit) or one (fp32) back has
+                    // read it.  With beta, lane L first brings column L of the chunk's C (contiguous
+                    // in memory) into the box, and every lane then replaces its row of C by D.
+                    constexpr int CB = 32 * 32 * static_cast<int>(sizeof(TD));   // bytes per box
+                    constexpr int NB = 4096 / CB;
+                    constexpr int COLB = CB / 32;                                  // bytes per box column
+                    const int nrow0 = j.n0 + quarter * 32;
+                    const bool use_c = j.beta != 0.0f && j.C != nullptr;
+                    for (int c = 0; c < chunks && ok; ++c) {
+                        const int m = j.m0 + c * 32;
+                        if (lane == 0) {
+                            if constexpr (NB == 2) ptx::bulk_wait_read1();
+                            else ptx::bulk_wait_read0();
+                        }
+                        __syncwarp();
+                        uint8_t* box = epi_stage + quarter * 4096 + (c % NB) * CB;
+                        const uint32_t ba = ptx::smem_u32(box);
+                        if (use_c) {
+                            const int ccol = m + lane;
+                            if (ccol < j.M) {
+                                const int64_t cbase = static_cast<int64_t>(j.b) * p.stride_c +
+                                                      static_cast<int64_t>(ccol) * j.ldc + nrow0;
+                                const char* src = static_cast<const char*>(j.C) + cbase * static_cast<int64_t>(sizeof(TD));
+                                if (nrow0 + 32 <= j.N && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+                                    // every load of the column is in flight before the first store
+                                    uint4 v4[COLB / 16];
+#pragma unroll
+                                    for (int q = 0; q < COLB / 16; ++q) v4[q] = __ldg(reinterpret_cast<const uint4*>(src) + q);
+#pragma unroll
+                                    for (int q = 0; q < COLB / 16; ++q)
+                                        ptx::st_shared_v4(ba + static_cast<uint32_t>(lane * COLB + q * 16), v4[q].x, v4[q].y,
+                                                          v4[q].z, v4[q].w);
+                                } else {
+#pragma unroll 1
+                                    for (int rr = 0; rr < 32; ++rr) {
+                                        const float cv = (nrow0 + rr < j.N) ? Out<TD>::load(j.C, cbase + rr) : 0.f;
+                                        const uint32_t a = ba + static_cast<uint32_t>(lane * COLB + rr * static_cast<int>(sizeof(TD)));
+                                        if constexpr (sizeof(TD) == 4) ptx::st_shared_u32(a, __float_as_uint(cv));
+                                        else if constexpr (std::is_same<TD, __half>::value)
+                                            ptx::st_shared_u16(a, __half_as_ushort(__float2half_rn(cv)));
+                                        else ptx::st_shared_u16(a, static_cast<uint16_t>(__float_as_uint(cv) >> 16));
+                                    }
+                                }
+                            }
+                            __syncwarp();
+                        }
+                        uint32_t r[32];
+                        __syncwarp();
+                        ptx::tmem_ld32(tbase + c * 32, r);
+                        if (c == chunks - 1) release_tmem<CG>(&tempty[mbuf], lane);
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) {
+                            const uint32_t a = ba + static_cast<uint32_t>((i * 32 + lane) * static_cast<int>(sizeof(TD)));
+                            const float acc = __uint_as_float(r[i]);
+                            if constexpr (sizeof(TD) == 4) {
+                                const float o = use_c ? fmaf(j.alpha, acc, j.beta * __uint_as_float(ptx::ld_shared_u32(a)))
+                                                      : j.alpha * acc;
+                                ptx::st_shared_u32(a, __float_as_uint(o));
+                            } else {
+                                constexpr bool half = std::is_same<TD, __half>::value;
+                                float cf = 0.f;
+                                if (use_c) {
+                                    const uint32_t bits = ptx::ld_shared_u16(a);
+                                    cf = half ? __half2float(__ushort_as_half(static_cast<unsigned short>(bits)))
+                                              : __uint_as_float(bits << 16);
+                                }
+                                const float o = use_c ? fmaf(j.alpha, acc, j.beta * cf) : j.alpha * acc;
+                                uint16_t ob;
+                                if constexpr (half) ob = __half_as_ushort(__float2half_rn(o));
+                                else ob = p.out_trunc ? static_cast<uint16_t>(__float_as_uint(o) >> 16)
+                                                      : __bfloat16_as_ushort(__float2bfloat16_rn(o));
+                                ptx::st_shared_u16(a, ob);
+                            }
+                        }
+                        ptx::fence_proxy_async_smem();
+                        __syncwarp();
+                        if (lane == 0 && m < j.M && nrow0 < j.N) {
+                            ptx::tma_store_3d(j.tmD, box, nrow0, m, j.b);
+                            ptx::bulk_commit();
+                        }
+                    }
+                    if (tr) trace_mark(p, TL_TRACE_STORED);
+                    mbuf ^= 1u;
+                    if (mbuf == 0) mph ^= 1u;
+                    continue;
+                }
+            }
             if (j.nsplit == 1 && j.tmD != nullptr && !direct) {
                 // each warp stages its 32 rows x 128 bytes of output (128-byte swizzle: 16-byte unit
                 // u of row r sits at u ^ (r & 7)) and writes them with one TMA store; the tensor

@@ -216,6 +216,62 @@ void simt_solution(tl_gemm_solution* s)
 bool m_mn_major(const tl_gemm_problem& p) { return p.trans_a == TL_OP_N; }   // A[m + k*lda]
 bool n_mn_major(const tl_gemm_problem& p) { return p.trans_b == TL_OP_T; }   // B[n + k*ldb]
 
+// NN problems on the tensor cores run as their transposed product D^T = B^T A^T (a TT problem:
+// m and n, A and B exchanged) whose output the epilogue stores transposed, i.e. straight into the
+// caller's column-major D.  An MN-major operand on the MMA's N side (the problem's m side: A of an
+// NN problem) costs ~9 % at 4096^3 (NN and NT 1557 TFLOP/s against TN and TT 1700); on the M side
+// it costs nothing, and the exchange puts it there.  Only with beta == 0, k >= 2048 and without
+// explicit split-k: the transposed epilogue reads C and finishes split tiles element by element
+// across a warp, which measured slower than the exchange gains, and with short k its epilogue
+// weighs more (4096 x 4096 x 1024: 31.4 against 30.5 us).  Not with a fused epilogue (its bias and amax
+// follow the problem's m) nor fp8 (no MN-major fp8 operands).  TL_NN_TRANSPOSE=0 turns it off.
+bool nn_view_enabled()
+{
+    static const bool on = [] {
+        const char* e = getenv("TL_NN_TRANSPOSE");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+bool tc_nn_view(const tl_gemm_problem& p, int kernel)
+{
+    return nn_view_enabled() && kernel == TL_KERNEL_TCGEN05 && p.trans_a == TL_OP_N && p.trans_b == TL_OP_N &&
+           p.beta == 0.0f && p.k >= 2048 && (p.dtype_a == TL_DTYPE_FP16 || p.dtype_a == TL_DTYPE_BF16) &&
+           p.dtype_d != TL_DTYPE_FP8_E4M3;
+}
+// The kernel's view of an NN problem: C, D, their leading dimensions and strides stay the caller's.
+tl_gemm_problem nn_view(const tl_gemm_problem& p)
+{
+    tl_gemm_problem q = p;
+    q.m = p.n;
+    q.n = p.m;
+    q.trans_a = TL_OP_T;
+    q.trans_b = TL_OP_T;
+    q.lda = p.ldb;
+    q.ldb = p.lda;
+    q.stride_a = p.stride_b;
+    q.stride_b = p.stride_a;
+    return q;
+}
+void tc_heuristic(const tl_handle* h, const tl_gemm_problem& p, int kernel, tl_gemm_solution* s);
+// A view's solution without explicit split-k keeps the view.
+bool view_solution_ok(const tl_gemm_solution& s) { return s.split_k <= 1; }
+// The heuristic for a problem that may run as its view: the view's pick when it needs no split-k,
+// else the caller's problem's pick (*view reports which).
+void tc_heuristic_viewed(const tl_handle* h, const tl_gemm_problem& p, int kernel, bool allow, tl_gemm_solution* s,
+                         bool* view)
+{
+    *view = false;
+    if (allow && tc_nn_view(p, kernel)) {
+        tc_heuristic(h, nn_view(p), kernel, s);
+        if (view_solution_ok(*s)) {
+            *view = true;
+            return;
+        }
+    }
+    tc_heuristic(h, p, kernel, s);
+}
+
 // Two CTA pairs per cluster (macro_tile1 512) load the shared m-side operand with a TMA multicast
 // copy.  That copy is kept to memory of the GPU running the kernel: an operand must be device (or
 // managed) memory of `device`, as cudaPointerGetAttributes reports it -- not host memory, another
@@ -352,6 +408,9 @@ void tc_heuristic(const tl_handle* h, const tl_gemm_problem& p, int kernel, tl_g
         for (int bm : {256, 128, 192, 64})
             for (int split : {1, 2, 3, 4, 6, 8, 12, 16}) {
                 if (cg == 4 && !cluster4_enabled()) continue;
+                // two pairs sharing a K-major 16-bit m-side operand measured 1-10 % slower than a
+                // pair (TN 4096^3 86.2 against 78.5 us, TN 1024 x 4096 x 4096 28.2 against 27.4)
+                if (cg == 4 && !m_mn_major(p) && in != TL_DTYPE_FP8_E4M3) continue;
                 if (split > 1 && (split > num_kb / 2 || split > 16)) continue;
                 c.macro_tile0 = bm;
                 c.macro_tile1 = kTcTileN * cg;
@@ -522,6 +581,7 @@ struct Prepared {
     size_t part_bytes = 0;
     tl_epilogue epi{};
     bool epi_on = false;
+    bool tview = false;      // p is the transposed view of the caller's NN problem (tc_nn_view)
 };
 
 int64_t operand_span(int64_t ld, int64_t cols, int64_t batch, int64_t bstride, int64_t rows)
@@ -531,7 +591,7 @@ int64_t operand_span(int64_t ld, int64_t cols, int64_t batch, int64_t bstride, i
 }
 
 tl_status prepare(tl_handle* h, const tl_gemm_problem* prob, const tl_gemm_solution* sol, void* D, const void* C,
-                  const void* A, const void* B, Prepared* out)
+                  const void* A, const void* B, Prepared* out, bool epilogue = false)
 {
     tl_status st = bind_thread(h);
     if (st != TL_SUCCESS) return st;
@@ -546,23 +606,35 @@ tl_status prepare(tl_handle* h, const tl_gemm_problem* prob, const tl_gemm_solut
     if (p.k > 0 && p.m > 0 && p.n > 0 && (!A || !B)) return fail(TL_ERR_INVALID_ARG, "A or B is NULL");
 
     int kernel = resolve_kernel(p);
+    bool view = false;
     if (sol) {
         P.s = *sol;
         if (P.s.kernel == TL_KERNEL_AUTO) P.s.kernel = kernel;
         kernel = P.s.kernel;
         if (p.kernel != TL_KERNEL_AUTO && kernel != p.kernel)
             return fail(TL_ERR_INVALID_ARG, "solution kernel differs from the problem's kernel request");
+        view = !epilogue && tc_nn_view(p, kernel) && view_solution_ok(P.s);
     } else {
         std::lock_guard<std::mutex> g(h->mu);
         auto it = h->tuned.find(problem_key(h, p));
         if (it != h->tuned.end()) {
             P.s = it->second;
             kernel = P.s.kernel;
+            view = !epilogue && tc_nn_view(p, kernel) && view_solution_ok(P.s);
         } else if (kernel == TL_KERNEL_SIMT) {
             simt_solution(&P.s);
         } else {
-            tc_heuristic(h, p, kernel, &P.s);
+            tc_heuristic_viewed(h, p, kernel, !epilogue, &P.s, &view);
         }
+    }
+    // an NN problem runs as its transposed view from here on (solutions are for the view)
+    if (view) {
+        P.p = nn_view(*prob);
+        P.A = B;
+        P.B = A;
+        A = P.A;
+        B = P.B;
+        P.tview = true;
     }
     // operands the TMA cannot describe fall back to the SIMT kernel when the caller left it to us
     std::string why;
@@ -571,6 +643,12 @@ tl_status prepare(tl_handle* h, const tl_gemm_problem* prob, const tl_gemm_solut
         if (p.kernel == TL_KERNEL_AUTO && !sol && p.dtype_d != TL_DTYPE_FP8_E4M3) {
             kernel = TL_KERNEL_SIMT;
             simt_solution(&P.s);
+            if (P.tview) {            // the CUDA-core kernel takes the caller's problem as it is
+                P.p = *prob;
+                P.A = B;
+                P.B = A;
+                P.tview = false;
+            }
         } else {
             return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel: " + why);
         }
@@ -763,6 +841,7 @@ tl_status enqueue(tl_handle* h, const Prepared& P, cudaStream_t s)
     L.epi_bias_dtype = P.epi.bias_dtype;
     L.epi_act = P.epi.activation;
     L.debug_flags = P.s.debug_flags;
+    L.out_t = P.tview ? 1 : 0;
     const bool timed = timing_begin(h, s);
     const tl_status st = tc_gemm_launch(L, s, &h->launches);
     timing_end(h, s, timed, st);
@@ -852,7 +931,24 @@ tl_status plan_tc_noalloc(int device, int sm_count, size_t smem_optin, const tl_
 {
     tl_status st = validate(prob);
     if (st != TL_SUCCESS) return st;
-    const tl_gemm_problem& p = *prob;
+    // NN problems run as their transposed view where tl_gemm runs them so (same sums, same results)
+    tl_gemm_solution s;
+    bool tview = false;
+    {
+        tl_handle probe;           // host-side device description only
+        probe.sm_count = sm_count;
+        probe.smem_optin = smem_optin;
+        if (sol) {
+            s = *sol;
+            if (s.kernel == TL_KERNEL_AUTO) s.kernel = TL_KERNEL_TCGEN05;
+            tview = tc_nn_view(*prob, TL_KERNEL_TCGEN05) && view_solution_ok(s);
+        } else {
+            tc_heuristic_viewed(&probe, *prob, TL_KERNEL_TCGEN05, true, &s, &tview);
+        }
+    }
+    const tl_gemm_problem view = tview ? nn_view(*prob) : *prob;
+    if (tview) std::swap(A, B);
+    const tl_gemm_problem& p = view;
     if (p.kernel != TL_KERNEL_AUTO && p.kernel != TL_KERNEL_TCGEN05)
         return fail(TL_ERR_UNSUPPORTED, "tl_gemm_noalloc runs the tcgen05 kernel only");
     if (p.dtype_a != TL_DTYPE_FP16 && p.dtype_a != TL_DTYPE_BF16 && p.dtype_a != TL_DTYPE_FP8_E4M3)
@@ -865,14 +961,7 @@ tl_status plan_tc_noalloc(int device, int sm_count, size_t smem_optin, const tl_
     tl_handle dev;                 // host-side device description only; holds no device memory
     dev.sm_count = sm_count;
     dev.smem_optin = smem_optin;
-    tl_gemm_solution s;
-    if (sol) {
-        s = *sol;
-        if (s.kernel == TL_KERNEL_AUTO) s.kernel = TL_KERNEL_TCGEN05;
-        if (s.kernel != TL_KERNEL_TCGEN05) return fail(TL_ERR_UNSUPPORTED, "tl_gemm_noalloc: solution must be TCGEN05");
-    } else {
-        tc_heuristic(&dev, p, TL_KERNEL_TCGEN05, &s);
-    }
+    if (sol && s.kernel != TL_KERNEL_TCGEN05) return fail(TL_ERR_UNSUPPORTED, "tl_gemm_noalloc: solution must be TCGEN05");
     if (s.macro_tile1 == 4 * kTcTileN && p.m > 0 && p.n > 0 && p.k > 0 && !multicast_ok(A, B, device)) {
         if (sol) return multicast_refused();
         drop_cluster4(&dev, &s);
@@ -907,6 +996,7 @@ tl_status plan_tc_noalloc(int device, int sm_count, size_t smem_optin, const tl_
     L->epi_on = p.dtype_d == TL_DTYPE_FP8_E4M3 ? 1 : 0;     // fp8 outputs come out of the epilogue kernels
     L->epi_dscale = 1.0f;
     L->sm_count = sm_count;
+    L->out_t = tview ? 1 : 0;
     return TL_SUCCESS;
 }
 
@@ -1058,8 +1148,9 @@ TL_API tl_status tl_default_solution(tl_handle* h, const tl_gemm_problem* p, tl_
     tl_status st = validate(p);
     if (st != TL_SUCCESS) return st;
     const int kernel = resolve_kernel(*p);
+    bool view = false;
     if (kernel == TL_KERNEL_SIMT) simt_solution(s);
-    else tc_heuristic(h, *p, kernel, s);
+    else tc_heuristic_viewed(h, *p, kernel, true, s, &view);
     return TL_SUCCESS;
 }
 
@@ -1079,7 +1170,7 @@ TL_API tl_status tl_check_solution(tl_handle* h, const tl_gemm_problem* p, const
         return fail(TL_ERR_UNSUPPORTED, "bf16x3/bf16x6 need fp32 inputs");
     if (s->kernel == TL_KERNEL_TCGEN05 && p->dtype_a == TL_DTYPE_FP32)
         return fail(TL_ERR_UNSUPPORTED, "tcgen05 kernel needs fp16/bf16/fp8 inputs");
-    return check_tc_solution(h, *p, *s);
+    return check_tc_solution(h, tc_nn_view(*p, s->kernel) && view_solution_ok(*s) ? nn_view(*p) : *p, *s);
 }
 
 TL_API tl_status tl_gemm(tl_handle* h, const tl_gemm_problem* p, const tl_gemm_solution* s, void* D, const void* C,
@@ -1209,7 +1300,7 @@ TL_API tl_status tl_gemm_ex(tl_handle* h, const tl_gemm_problem* p, const tl_epi
     Prepared P;
     t_capturing = stream_capturing(S(stream));
     if (t_capturing) h->captured = true;
-    tl_status st = prepare(h, p, s, D, C, A, B, &P);
+    tl_status st = prepare(h, p, s, D, C, A, B, &P, true);
     t_capturing = false;
     if (st != TL_SUCCESS) return st;
     if (P.kernel == TL_KERNEL_SIMT)
@@ -1238,7 +1329,7 @@ TL_API tl_status tl_tune(tl_handle* h, const tl_gemm_problem* p, void* D, const 
         simt_solution(&s);
         cands.push_back(s);
     } else {
-        cands = tc_candidates(h, *p, kernel);
+        cands = tc_candidates(h, tc_nn_view(*p, kernel) ? nn_view(*p) : *p, kernel);
     }
     // the multicast variant only where A and B are this GPU's memory
     if (!multicast_ok(A, B, h->device))

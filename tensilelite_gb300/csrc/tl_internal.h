@@ -103,6 +103,7 @@ struct TcLaunch {
     int debug_flags;         // tl_gemm_solution.debug_flags (TL_DEBUG_SKIP_LOADS)
     unsigned long long* trace;   // device timeline (tl_set_trace) or null
     int64_t trace_bytes;
+    int out_t;               // D and C hold the transpose of this launch's output (NN run as TT)
 };
 
 // Dynamic shared memory of one CTA staging bm_cta m-rows per stage (bm / 2 for a CTA pair).
