@@ -408,9 +408,6 @@ void tc_heuristic(const tl_handle* h, const tl_gemm_problem& p, int kernel, tl_g
         for (int bm : {256, 128, 192, 64})
             for (int split : {1, 2, 3, 4, 6, 8, 12, 16}) {
                 if (cg == 4 && !cluster4_enabled()) continue;
-                // two pairs sharing a K-major 16-bit m-side operand measured 1-10 % slower than a
-                // pair (TN 4096^3 86.2 against 78.5 us, TN 1024 x 4096 x 4096 28.2 against 27.4)
-                if (cg == 4 && !m_mn_major(p) && in != TL_DTYPE_FP8_E4M3) continue;
                 if (split > 1 && (split > num_kb / 2 || split > 16)) continue;
                 c.macro_tile0 = bm;
                 c.macro_tile1 = kTcTileN * cg;

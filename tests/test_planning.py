@@ -69,9 +69,9 @@ def test_planning_handle_refuses_device_work(gb300):
 DEVICE_PICKS = [
     ("bf16 4096^3 NN beta 0.5", dict(m=4096, n=4096, k=4096, beta=0.5), (256, 256, 1, 6, 0, 0, 64)),
     ("bf16 4096x4096x1024 NN", dict(m=4096, n=4096, k=1024), (256, 512, 1, 6, 0, 0, 64)),
-    ("bf16 dX 1024x4096x4096 TN", dict(m=1024, n=4096, k=4096, trans_a=True), (256, 256, 1, 6, 0, 0, 64)),
+    ("bf16 dX 1024x4096x4096 TN", dict(m=1024, n=4096, k=4096, trans_a=True), (256, 512, 1, 6, 0, 0, 64)),
     ("bf16 dW 4096x1024x4096 NT", dict(m=4096, n=1024, k=4096, trans_b=True), (256, 512, 1, 6, 0, 0, 64)),
-    ("bf16 1024x4096x4096 NN", dict(m=1024, n=4096, k=4096), (256, 256, 1, 6, 0, 0, 64)),
+    ("bf16 1024x4096x4096 NN", dict(m=1024, n=4096, k=4096), (256, 512, 1, 6, 0, 0, 64)),
     ("bf16 480x1024x4096 NN", dict(m=480, n=1024, k=4096), (128, 128, 4, 6, 0, 0, 64)),
     ("bf16 1024^3 NN", dict(m=1024, n=1024, k=1024), (128, 256, 1, 6, 0, 0, 64)),
     ("bf16 1024x1024x4096 NN", dict(m=1024, n=1024, k=4096), (192, 128, 3, 5, 0, 0, 64)),
