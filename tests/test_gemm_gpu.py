@@ -197,6 +197,20 @@ def test_split_k_reductions(h, cg, bm, split):
 
 
 @pytest.mark.parametrize("od", ["bf16", "fp16", "fp32"])
+@pytest.mark.parametrize("m,n,k", [(1000, 600, 2048), (2048, 2048, 4096), (4096, 264, 2048)])
+def test_nn_runs_transposed(h, od, m, n, k):
+    """NN with beta = 0 and k >= 2048 runs as the transposed TT product with a transposed store
+    (32 x 32 TMA boxes; ragged edges; 2048^2 leaves a partial wave, whose balanced split finishes
+    its tiles element by element).  Every output type against the oracle."""
+    dt = "fp16" if od == "fp16" else "bf16"
+    case = gg.make_case(dt, "NN", 1500 + m + n, m, n, k, alpha=1.5, beta=0.0, ld_align=8)
+    got = gu.run_case(h, case, kernel="tcgen05", dtype=dt, out_dtype=od)
+    G = gu.mat(got, m, n, case["ldc"])
+    R = gu.mat(gu.oracle_ref(case), m, n, m)
+    assert_close(G, R, absprod_of(case), k, case["alpha"], 0.0, None, od)
+
+
+@pytest.mark.parametrize("od", ["bf16", "fp16", "fp32"])
 @pytest.mark.parametrize("m", [480, 479])
 def test_parallel_split_k_c_staging(h, od, m):
     """Parallel split-k with beta: a split copies the C rows of the chunk it finishes into shared

@@ -102,6 +102,20 @@ def test_heuristic_solutions_are_legal(gb300, dtype, ta, tb):
         gb300.check_solution(p, s)
 
 
+def test_nn_plans_as_its_transposed_view(gb300):
+    """An NN problem with beta = 0 and k >= 2048 is planned (and run) as the TT problem with m and n
+    exchanged; with beta != 0 or short k it is planned as it is."""
+    nn = Problem.make(1024, 4096, 4096, dtype="bf16")
+    tt = Problem.make(4096, 1024, 4096, dtype="bf16", trans_a=True, trans_b=True)
+    assert gb300.default_solution(nn).as_dict() == gb300.default_solution(tt).as_dict()
+    gb300.check_solution(nn, gb300.default_solution(nn))
+    # with beta, or k below 2048, the NN problem keeps its own shape: a pick that is legal only for
+    # it (MN-major A needs whole 128-byte chunks of m per CTA) is accepted
+    for p in (Problem.make(1024, 4096, 4096, dtype="bf16", beta=0.5), Problem.make(1024, 4096, 1024, dtype="bf16")):
+        s = gb300.default_solution(p)
+        gb300.check_solution(p, s)
+
+
 def test_heuristic_is_deterministic_and_simt_for_fp32(gb300):
     p = Problem.make(3000, 2000, 1000, dtype="bf16")
     assert gb300.default_solution(p).as_dict() == gb300.default_solution(p).as_dict()
