@@ -18,11 +18,12 @@ cast to bf16 (RNE), fp32 accumulation, bf16 output.  One step = one GEMM launch.
              a bounded sample of output columns of the same problem, all host threads, and on one
              thread as the reference runs it; the host's CPU model is named.
   suite      (default run only) the other configurations, measured after the headline: fp16 and the
-             other bf16 layouts at 4096^3, bf16 480x1024x4096, fp8 8192^3, the 256-problem grouped
+             other bf16 layouts at 4096^3 (and NN with beta = 0, which runs as the transposed TT
+             product), bf16 480x1024x4096, fp8 8192^3, the 256-problem grouped
              launch, forward+backward, bf16x3 / bf16x6 / CUDA-core fp32 at 8192^3 and the CUDA-core
              480x512x512 case -- throughput, roofline fraction and FP64 error of each.
 
-Other workloads (--workload): fp16_4096_nn|nt|tn, bf16_4096_nt|tn, bf16_480x1024x4096, bf16x3_8192,
+Other workloads (--workload): fp16_4096_nn|nt|tn, bf16_4096_nt|tn|nn_b0, bf16_480x1024x4096, bf16x3_8192,
 simt_fp32_8192, fp8_8192, grouped256, fwdbwd.  `--impl reference` times the reference's CPU loop
 (the oracle port) on the same workload instead.
 
@@ -57,6 +58,7 @@ L2_BYTES = 129e6      # GB300 L2
 # ----------------------------------------------------------------------------------------------
 WORKLOADS = {
     "bf16_4096_nn": dict(dtype="bf16", m=4096, n=4096, k=4096, lay="NN", alpha=1.0, beta=0.5, seed=1, dist="normal"),
+    "bf16_4096_nn_b0": dict(dtype="bf16", m=4096, n=4096, k=4096, lay="NN", alpha=1.0, beta=0.0, seed=1, dist="normal"),
     "bf16_4096_nt": dict(dtype="bf16", m=4096, n=4096, k=4096, lay="NT", alpha=1.0, beta=0.5, seed=1, dist="normal"),
     "bf16_4096_tn": dict(dtype="bf16", m=4096, n=4096, k=4096, lay="TN", alpha=1.0, beta=0.5, seed=1, dist="normal"),
     "fp16_4096_nn": dict(dtype="fp16", m=4096, n=4096, k=4096, lay="NN", alpha=1.0, beta=0.5, seed=1, dist="normal"),
@@ -1006,7 +1008,7 @@ def run_reference(args, w, name):
 # its line under "suite" (device throughput, roofline fraction, FP64 error; no e2e or CPU legs):
 # (workload, timed steps, warm-up steps)
 SUITE = [
-    ("fp16_4096_nn", 100, 10), ("bf16_4096_tn", 100, 10), ("bf16_4096_nt", 100, 10),
+    ("fp16_4096_nn", 100, 10), ("bf16_4096_nn_b0", 100, 10), ("bf16_4096_tn", 100, 10), ("bf16_4096_nt", 100, 10),
     ("bf16_480x1024x4096", 2000, 20), ("fp8_8192", 50, 5), ("grouped256", 100, 5), ("fwdbwd", 200, 10),
     ("bf16x3_8192", 20, 3), ("bf16x6_8192", 20, 3), ("simt_fp32_8192", 4, 3), ("simt_fp32_480x512x512", 2000, 20),
 ]
