@@ -220,8 +220,8 @@ bool n_mn_major(const tl_gemm_problem& p) { return p.trans_b == TL_OP_T; }   // 
 // m and n, A and B exchanged) whose output the epilogue stores transposed, i.e. straight into the
 // caller's column-major D.  An MN-major operand on the MMA's N side (the problem's m side: A of an
 // NN problem) costs ~9 % at 4096^3 (NN and NT 1557 TFLOP/s against TN and TT 1700); on the M side
-// it costs nothing, and the exchange puts it there.  Only with beta == 0, k >= 2048 and without
-// explicit split-k: the transposed epilogue reads C and finishes split tiles element by element
+// it costs nothing, and the exchange puts it there.  Only for one GEMM (batch 1, the measured
+// case), with beta == 0, k >= 2048 and without explicit split-k: the transposed epilogue reads C and finishes split tiles element by element
 // across a warp, which measured slower than the exchange gains, and with short k its epilogue
 // weighs more (4096 x 4096 x 1024: 31.4 against 30.5 us).  Not with a fused epilogue (its bias and amax
 // follow the problem's m) nor fp8 (no MN-major fp8 operands).  TL_NN_TRANSPOSE=0 turns it off.
@@ -236,7 +236,7 @@ bool nn_view_enabled()
 bool tc_nn_view(const tl_gemm_problem& p, int kernel)
 {
     return nn_view_enabled() && kernel == TL_KERNEL_TCGEN05 && p.trans_a == TL_OP_N && p.trans_b == TL_OP_N &&
-           p.beta == 0.0f && p.k >= 2048 && (p.dtype_a == TL_DTYPE_FP16 || p.dtype_a == TL_DTYPE_BF16) &&
+           p.beta == 0.0f && p.k >= 2048 && p.batch == 1 && (p.dtype_a == TL_DTYPE_FP16 || p.dtype_a == TL_DTYPE_BF16) &&
            p.dtype_d != TL_DTYPE_FP8_E4M3;
 }
 // The kernel's view of an NN problem: C, D, their leading dimensions and strides stay the caller's.
