@@ -30,7 +30,9 @@ def test_no_undeclared_exports():
 
 def _c_sizeof(expr):
     src = f'#include "include/tensilelite.h"\n#include <stdio.h>\n#include <stddef.h>\nint main(){{printf("%zu", (size_t)({expr}));}}'
-    exe = os.path.join("/tmp", "tl_sizeof_probe")
+    build = os.path.join(ROOT, "tensilelite_gb300", "_build")     # the package's (git-ignored) build folder
+    os.makedirs(build, exist_ok=True)
+    exe = os.path.join(build, "tl_sizeof_probe")
     r = subprocess.run(["gcc", "-x", "c", "-I", ROOT, "-o", exe, "-"], input=src, text=True, capture_output=True,
                        cwd=ROOT)
     assert r.returncode == 0, r.stderr
