@@ -110,7 +110,11 @@ typedef struct tl_gemm_problem {
  * across CTAs and reduces through a device workspace owned by the handle.
  * promote_k > 0 (TCGEN05/BF16X3/BF16X6 with macro_tile0 == 128): the dominant product restarts its
  * tensor-core accumulation every promote_k elements of k and the chains are summed in fp32 on the
- * CUDA cores (tensor-core accumulation error grows with the chain length). */
+ * CUDA cores (tensor-core accumulation error grows with the chain length).
+ * A single fp16/bf16 NN problem with beta == 0, k >= 2048 and split_k <= 1 runs on TCGEN05 as its
+ * transposed product (D^T = B^T A^T, a TT problem, stored transposed into D): there the solution
+ * describes that product, so macro_tile0 tiles n and macro_tile1 m (TL_NN_TRANSPOSE=0 turns this
+ * off). */
 typedef struct tl_gemm_solution {
     int32_t kernel;            /* resolved tl_kernel (never AUTO once filled in) */
     int32_t macro_tile0;
