@@ -55,3 +55,24 @@ def test_reference_arm_rank0_only(rank):
         line = json.loads(lines[-1])
         assert line["impl"] == "reference" and line["unit"] == "TFLOP/s" and line["value"] > 0
         assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_reference_arm_line_carries_the_contract_keys():
+    """One process (no WORLD_SIZE): the reference arm's line has every key of the bench contract,
+    on the workload and metric of the GPU arm's headline."""
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    env["CUDA_VISIBLE_DEVICES"] = ""
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "3"], cwd=ROOT,
+                       env=env, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr
+    line = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+                "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["n_gpus"] == 1 and line["steps"] == 1 and line["warmup"] >= 3
+    assert line["higher_is_better"] is True and line["unit"] == "TFLOP/s" and line["value"] > 0
+    assert line["config"]["workload"].startswith("bf16_4096_nn")
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
+    assert line["e2e"]["value"] == line["value"] and line["e2e"]["h2d_bytes_per_step"] == 0
+    assert line["e2e"]["d2h_bytes_per_step"] == 0
